@@ -1,0 +1,183 @@
+/*
+ * nsg.h — C ABI of libnsg.so, the GB300-native (sm_103a) implementation of
+ * nscale's nuclei-segmentation hot path.
+ *
+ * Every entry point replaces one reference interface (cited per function;
+ * paths relative to the nscale tree).  All image arguments are DEVICE
+ * pointers to dense row-major arrays (row stride == cols elements) unless a
+ * function says otherwise; sizes are plain ints; no C++ type crosses the ABI.
+ * Work is enqueued on the caller's CUDA stream (`stream` is a cudaStream_t,
+ * NULL = legacy default stream).  Functions that return a count to the host
+ * synchronise that stream, as the reference returns those counts by value.
+ *
+ * Status codes: the pipeline returns the reference's own values
+ * (HistologicalEntities.h:34-40); library failures are negative NSG_ERR_*.
+ * No C++ exception crosses the ABI.
+ *
+ * Threading: a context (workspace arena) may be used by one host thread at a
+ * time; independent contexts are independent.
+ */
+#ifndef NSG_H
+#define NSG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status values of nscale::HistologicalEntities (HistologicalEntities.h:34-40) */
+#define NSG_SUCCESS 0
+#define NSG_BACKGROUND 1
+#define NSG_BACKGROUND_LIKELY 2
+#define NSG_NO_CANDIDATES_LEFT 3
+#define NSG_CONTINUE 4
+#define NSG_INVALID_IMAGE (-1)
+#define NSG_RUNTIME_FAILED (-2)
+/* library errors */
+#define NSG_ERR_ARG (-10)        /* bad argument (size, connectivity, NULL pointer) */
+#define NSG_ERR_OOM (-11)        /* device allocation failed / image larger than the context */
+#define NSG_ERR_TIMEOUT (-12)    /* a device-side wait exceeded its iteration budget */
+#define NSG_ERR_QUEUE_FULL (-13) /* a device queue overflowed its capacity */
+#define NSG_ERR_CUDA (-14)       /* a CUDA runtime call failed */
+#define NSG_ERR_UNSUPPORTED (-15)
+
+typedef struct nsg_context nsg_context;
+typedef void *nsg_stream_t; /* cudaStream_t */
+
+/* Parameters of segmentNuclei, same order, meaning and defaults as
+ * HistologicalEntities.h:52-54 (logger / intermediate-result handler are
+ * replaced by nsg_context_set_dump). */
+typedef struct nsg_seg_params {
+    int blue, green, red;       /* 220 220 220 */
+    double T1, T2;              /* 5.0 4.0 */
+    int G1;                     /* 80 */
+    int minSize, maxSize;       /* 11 1000 */
+    int G2;                     /* 45 */
+    int minSizePl;              /* 30 */
+    int minSizeSeg, maxSizeSeg; /* 21 1000 */
+    int fillHolesConnectivity;  /* 4 */
+    int reconConnectivity;      /* 8 */
+    int watershedConnectivity;  /* 8 */
+} nsg_seg_params;
+
+int nsg_version(void);
+void nsg_default_params(nsg_seg_params *p);
+const char *nsg_status_string(int status);
+
+/* Workspace arena for images up to max_rows x max_cols on `device`.  All
+ * scratch memory the library needs is allocated here, once; no call below
+ * allocates device memory. */
+int nsg_context_create(nsg_context **ctx, int max_rows, int max_cols, int device);
+int nsg_context_destroy(nsg_context *ctx);
+const char *nsg_context_last_error(const nsg_context *ctx);
+size_t nsg_context_bytes(const nsg_context *ctx);
+/* Device-wait budget for persistent kernels (iterations); tests set it low to
+ * exercise NSG_ERR_TIMEOUT.  0 restores the default. */
+int nsg_context_set_spin_budget(nsg_context *ctx, long long iterations);
+
+/* ---- PixelOperations / HistologicalEntities helpers ---------------------- */
+/* HistologicalEntities::getBackground (HistologicalEntities.cpp:93-109):
+ * mask = (B > blue) & (G > green) & (R > red); *count = countNonZero. */
+int nsg_get_background(nsg_context *ctx, const uint8_t *bgr, int rows, int cols, int blue, int green, int red,
+                       uint8_t *mask_out /* nullable */, int64_t *count_out /* host, nullable */,
+                       nsg_stream_t stream);
+/* HistologicalEntities::getRBC (HistologicalEntities.cpp:33-81), FP32 as the
+ * CPU reference computes it. */
+int nsg_get_rbc(nsg_context *ctx, const uint8_t *bgr, int rows, int cols, double T1, double T2, uint8_t *rbc_out,
+                nsg_stream_t stream);
+/* PixelOperations::invert<unsigned char> (PixelOperations.cpp:22-43). */
+int nsg_invert_u8(nsg_context *ctx, const uint8_t *in, uint8_t *out, int64_t n, nsg_stream_t stream);
+
+/* ---- MorphologicOperations ------------------------------------------------ */
+/* cv::erode / cv::dilate with a k x k structuring element given in HOST
+ * memory (k odd, <= 31); out-of-image samples are neutral (255 for erode, 0
+ * for dilate), as morphOpen pads them (MorphologicOperations.cpp:3849-3882). */
+int nsg_morph_erode_u8(nsg_context *ctx, const uint8_t *in, uint8_t *out, int rows, int cols, const uint8_t *se,
+                       int k, nsg_stream_t stream);
+int nsg_morph_dilate_u8(nsg_context *ctx, const uint8_t *in, uint8_t *out, int rows, int cols, const uint8_t *se,
+                        int k, nsg_stream_t stream);
+/* nscale::morphOpen<unsigned char> (MorphologicOperations.cpp:3849-3882). */
+int nsg_morph_open_u8(nsg_context *ctx, const uint8_t *in, uint8_t *out, int rows, int cols, const uint8_t *se, int k,
+                      nsg_stream_t stream);
+
+/* nscale::imreconstruct<T>(seeds, image, conn) (MorphologicOperations.cpp:1731-1903). */
+int nsg_imreconstruct_u8(nsg_context *ctx, const uint8_t *marker, const uint8_t *mask, uint8_t *out, int rows,
+                         int cols, int conn, nsg_stream_t stream);
+int nsg_imreconstruct_f32(nsg_context *ctx, const float *marker, const float *mask, float *out, int rows, int cols,
+                          int conn, nsg_stream_t stream);
+/* nscale::imreconstructBinary<unsigned char> (MorphologicOperations.cpp:2769-2909). */
+int nsg_imreconstruct_binary_u8(nsg_context *ctx, const uint8_t *marker, const uint8_t *mask, uint8_t *out, int rows,
+                                int cols, int conn, nsg_stream_t stream);
+/* nscale::imfillHoles<unsigned char>(img, binary=true, conn) (MorphologicOperations.cpp:2940-3006). */
+int nsg_imfill_holes_u8(nsg_context *ctx, const uint8_t *img, uint8_t *out, int rows, int cols, int conn,
+                        nsg_stream_t stream);
+/* nscale::bwselect<unsigned char>(bw, seeds, conn) (MorphologicOperations.cpp:3010-3031). */
+int nsg_bwselect_u8(nsg_context *ctx, const uint8_t *bw, const uint8_t *seeds, uint8_t *out, int rows, int cols,
+                    int conn, nsg_stream_t stream);
+/* nscale::bwlabel2(img, conn, relab) (MorphologicOperations.cpp:3092-3117 over
+ * ConnComponents::label, ConnComponents.cpp:52-86): int32 labels, background
+ * -1, label = minimum raster index of the component. */
+int nsg_bwlabel(nsg_context *ctx, const uint8_t *img, int32_t *labels_out, int rows, int cols, int conn,
+                nsg_stream_t stream);
+/* nscale::bwareaopen2(img, false, true, min, max, conn, count)
+ * (MorphologicOperations.cpp:3281-3314, ConnComponents.cpp:205-239): keeps
+ * components with min <= area < max; *count_out (host) = kept components. */
+int nsg_bwareaopen(nsg_context *ctx, const uint8_t *img, uint8_t *out, int rows, int cols, int min_size,
+                   int max_size, int conn, int *count_out, nsg_stream_t stream);
+/* cv::distanceTransform(mask, dist, CV_DIST_L2, CV_DIST_MASK_PRECISE) as
+ * called at HistologicalEntities.cpp:359: exact Euclidean distance to the
+ * nearest zero pixel, float32. */
+int nsg_dist_transform(nsg_context *ctx, const uint8_t *mask, float *dist_out, int rows, int cols,
+                       nsg_stream_t stream);
+/* nscale::imhmin<float>(img, h, conn) (MorphologicOperations.cpp:3343-3364). */
+int nsg_imhmin_f32(nsg_context *ctx, const float *img, float *out, int rows, int cols, float h, int conn,
+                   nsg_stream_t stream);
+/* nscale::localMaxima<float> / localMinima<float>
+ * (MorphologicOperations.cpp:3764-3845): uint8 255 at regional extrema. */
+int nsg_local_maxima_f32(nsg_context *ctx, const float *img, uint8_t *out, int rows, int cols, int conn,
+                         nsg_stream_t stream);
+int nsg_local_minima_f32(nsg_context *ctx, const float *img, uint8_t *out, int rows, int cols, int conn,
+                         nsg_stream_t stream);
+/* nscale::watershed2(origImage, image, conn) (MorphologicOperations.cpp:3717-3760):
+ * minima labelling, OpenCV Meyer flooding with the reference's flooding
+ * order, border fix (NeighborOperations.cpp:18-44).  int32 output, -1 on
+ * watershed lines. */
+int nsg_watershed(nsg_context *ctx, const uint8_t *bgr, const float *img, int32_t *labels_out, int rows, int cols,
+                  int conn, nsg_stream_t stream);
+/* ConnComponents::boundingBox (ConnComponents.cpp:241-284) on a -1-background
+ * label image: writes compcount entries of (label, minx, maxx, miny, maxy) as
+ * five consecutive int32 arrays into HOST memory `bbox_out` (capacity
+ * 5*capacity ints); labels in increasing order (= first raster appearance). */
+int nsg_bounding_box(nsg_context *ctx, const int32_t *labels, int rows, int cols, int32_t *bbox_out, int capacity,
+                     int *compcount, nsg_stream_t stream);
+
+/* ---- HistologicalEntities::segmentNuclei ----------------------------------- */
+/* segmentNuclei(img, output, compcount, bbox, params...) (HistologicalEntities.cpp:473-598)
+ * and the mask-only overload (HistologicalEntities.cpp:600-664).
+ *  bgr:          DEVICE pointer, BGR interleaved uint8, row stride in bytes.
+ *  labels_out:   DEVICE int32 rows*cols (nullable): -1 background, label = min raster index.
+ *  mask_out:     DEVICE uint8 rows*cols (nullable): the filled final mask (255/0).
+ *  compcount:    HOST (nullable): number of components.
+ *  bbox:         HOST (nullable): *bbox receives an nsg_alloc'd int32[5*compcount]
+ *                (label, minx, maxx, miny, maxy arrays); free with nsg_free.
+ * Returns NSG_SUCCESS, NSG_BACKGROUND, NSG_BACKGROUND_LIKELY,
+ * NSG_NO_CANDIDATES_LEFT, NSG_INVALID_IMAGE or an NSG_ERR_* code.  On a non-
+ * SUCCESS status, labels_out is filled with -1 and mask_out with 0. */
+int nsg_segment_nuclei(nsg_context *ctx, const uint8_t *bgr, int rows, int cols, size_t row_stride_bytes,
+                       const nsg_seg_params *p, int32_t *labels_out, uint8_t *mask_out, int *compcount,
+                       int32_t **bbox, nsg_stream_t stream);
+/* Same pipeline from HOST memory: copies the tile in, runs, copies labels
+ * (and mask) back to HOST buffers (either nullable). */
+int nsg_segment_nuclei_host(nsg_context *ctx, const uint8_t *bgr_host, int rows, int cols, const nsg_seg_params *p,
+                            int32_t *labels_host, uint8_t *mask_host, int *compcount, int32_t **bbox,
+                            nsg_stream_t stream);
+
+void *nsg_alloc(size_t bytes);
+void nsg_free(void *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

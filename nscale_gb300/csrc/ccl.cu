@@ -1,0 +1,451 @@
+// ccl.cu — union-find connected components and everything built on them:
+//
+//  * bwlabel2 / ConnComponents::label        (MorphologicOperations.cpp:3092-3117,
+//                                             ConnComponents.cpp:52-86)
+//  * bwareaopen2 / areaThresholdLabeled       (MorphologicOperations.cpp:3281-3314,
+//                                             ConnComponents.cpp:205-239)
+//  * imreconstructBinary / bwselect / imfillHoles (binary)
+//                                            (MorphologicOperations.cpp:2769-3031)
+//  * ConnComponents::boundingBox              (ConnComponents.cpp:241-284)
+//
+// Labels follow the reference exactly: the root of every component is its
+// minimum raster index (the reference's merge() links the larger root under
+// the smaller, ConnComponents.cpp:34-43).  Here every pixel unions with its
+// already-visited neighbours (left, up, up-left, up-right) concurrently;
+// union hooks the larger root under the smaller with atomicMin and retries
+// when it lost a race, and find() halves paths.  Because hooking always goes
+// to a smaller index, the minimum index of a component is the only node that
+// can never be hooked, so the final roots are the reference's labels.
+//
+// Binary reconstruction has a unique answer — the mask components (under the
+// given connectivity) that contain a marker pixel — so imreconstructBinary,
+// bwselect and imfillHoles are all "label the mask, flag the components that
+// touch a seed (or the image border), select".
+#include <limits.h>
+
+#include "nsg_internal.cuh"
+
+namespace nsg {
+
+namespace {
+
+constexpr int kB = 256;
+
+__device__ __forceinline__ int find_root(int *parent, int x) {
+    for (;;) {
+        int p = __ldcg(parent + x);
+        if (p == x) return x;
+        int gp = __ldcg(parent + p);
+        if (gp != p) parent[x] = gp;  // path halving (benign race: ancestors only)
+        x = p;
+    }
+}
+
+__device__ __forceinline__ void unite(int *parent, int a, int b) {
+    for (int guard = 0; guard < 1 << 24; ++guard) {
+        a = find_root(parent, a);
+        b = find_root(parent, b);
+        if (a == b) return;
+        if (a < b) {
+            int t = a;
+            a = b;
+            b = t;
+        }
+        int old = atomicMin(parent + a, b);
+        if (old == a) return;
+        a = old;
+    }
+}
+
+template <int MODE>
+__device__ __forceinline__ bool fg(uint8_t v) {
+    return MODE == CCL_NOT255 ? v != 255 : v != 0;
+}
+template <int MODE>
+__device__ __forceinline__ bool joins(uint8_t a, uint8_t b) {
+    if (MODE == CCL_EQUAL) return a == b && a != 0;
+    if (MODE == CCL_NONZERO) return a != 0 && b != 0;
+    return a != 255 && b != 255;
+}
+
+template <int MODE>
+__global__ void ccl_init(const uint8_t *__restrict__ img, int *__restrict__ parent, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        parent[i] = fg<MODE>(img[i]) ? (int)i : -1;
+}
+
+template <int MODE>
+__global__ void ccl_merge(const uint8_t *__restrict__ img, int *parent, int rows, int cols, int conn) {
+    int64_t n = (int64_t)rows * cols;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint8_t p = img[i];
+        if (!fg<MODE>(p)) continue;
+        int y = (int)(i / cols), x = (int)(i - (int64_t)y * cols);
+        if (x > 0 && joins<MODE>(p, img[i - 1])) unite(parent, (int)i, (int)(i - 1));
+        if (y > 0) {
+            int64_t u = i - cols;
+            if (joins<MODE>(p, img[u])) unite(parent, (int)i, (int)u);
+            if (conn == 8) {
+                if (x > 0 && joins<MODE>(p, img[u - 1])) unite(parent, (int)i, (int)(u - 1));
+                if (x < cols - 1 && joins<MODE>(p, img[u + 1])) unite(parent, (int)i, (int)(u + 1));
+            }
+        }
+    }
+}
+
+__global__ void ccl_flatten(int *parent, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (__ldcg(parent + i) >= 0) parent[i] = find_root(parent, (int)i);
+    }
+}
+
+// float plateaus among valid pixels (local extrema floods)
+__global__ void cclf_init(const uint8_t *__restrict__ valid, int *__restrict__ parent, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        parent[i] = valid[i] ? (int)i : -1;
+}
+__global__ void cclf_merge(const float *__restrict__ val, const uint8_t *__restrict__ valid, int *parent, int rows,
+                           int cols, int conn) {
+    int64_t n = (int64_t)rows * cols;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (!valid[i]) continue;
+        float p = val[i];
+        int y = (int)(i / cols), x = (int)(i - (int64_t)y * cols);
+        if (x > 0 && valid[i - 1] && val[i - 1] == p) unite(parent, (int)i, (int)(i - 1));
+        if (y > 0) {
+            int64_t u = i - cols;
+            if (valid[u] && val[u] == p) unite(parent, (int)i, (int)u);
+            if (conn == 8) {
+                if (x > 0 && valid[u - 1] && val[u - 1] == p) unite(parent, (int)i, (int)(u - 1));
+                if (x < cols - 1 && valid[u + 1] && val[u + 1] == p) unite(parent, (int)i, (int)(u + 1));
+            }
+        }
+    }
+}
+
+__global__ void area_count(const int *__restrict__ lab, int *__restrict__ area, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int l = lab[i];
+        // warp-aggregate pixels of the same component
+        unsigned act = __activemask();
+        unsigned same = __match_any_sync(act, l);
+        int leader = __ffs(same) - 1;
+        if (l >= 0 && (threadIdx.x & 31) == leader) atomicAdd(area + l, __popc(same));
+    }
+}
+
+__global__ void area_select(const int *__restrict__ lab, const int *__restrict__ area, int64_t n, int lower,
+                            int upper, uint8_t *__restrict__ out, int *__restrict__ count) {
+    for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = i0 + threadIdx.x;
+        bool root_kept = false;
+        if (i < n) {
+            int l = lab[i];
+            bool keep = false;
+            if (l >= 0) {
+                int a = area[l];
+                keep = a >= lower && a < upper;
+                root_kept = keep && l == (int)i;
+            }
+            out[i] = keep ? 255 : 0;
+        }
+        unsigned b = __ballot_sync(0xffffffffu, root_kept);
+        if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, __popc(b));
+    }
+}
+
+// flag[root] |= seed present in the component
+__global__ void flag_seeds(const int *__restrict__ lab, const uint8_t *__restrict__ seed,
+                           const uint8_t *__restrict__ mask, int *__restrict__ flag, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int l = lab[i];
+        if (l >= 0 && seed[i] && mask[i] && !__ldcg(flag + l)) flag[l] = 1;
+    }
+}
+__global__ void flag_border(const int *__restrict__ lab, int *__restrict__ flag, int rows, int cols) {
+    int64_t nb = 2 * (int64_t)cols + 2 * (int64_t)rows;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nb; k += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i;
+        if (k < cols) i = k;
+        else if (k < 2 * cols) i = (int64_t)(rows - 1) * cols + (k - cols);
+        else if (k < 2 * cols + rows) i = (int64_t)(k - 2 * cols) * cols;
+        else i = (int64_t)(k - 2 * cols - rows) * cols + (cols - 1);
+        int l = lab[i];
+        if (l >= 0) flag[l] = 1;
+    }
+}
+__global__ void zero_flags_at_roots(const int *__restrict__ lab, int *__restrict__ flag, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (lab[i] == (int)i) flag[i] = 0;
+}
+// imreconstructBinary: marker pixels keep their value, reached mask pixels 255
+__global__ void select_recon(const int *__restrict__ lab, const int *__restrict__ flag,
+                             const uint8_t *__restrict__ marker, const uint8_t *__restrict__ mask,
+                             uint8_t *__restrict__ out, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint8_t mk = marker[i];
+        int l = lab[i];
+        out[i] = mk ? mk : ((mask[i] && l >= 0 && flag[l]) ? 255 : 0);
+    }
+}
+// bwselect: bw value on selected components
+__global__ void select_bw(const int *__restrict__ lab, const int *__restrict__ flag, const uint8_t *__restrict__ bw,
+                          uint8_t *__restrict__ out, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int l = lab[i];
+        out[i] = (l >= 0 && flag[l]) ? bw[i] : 0;
+    }
+}
+// imfillHoles: pixels reached from the border through (img != 255) become 0,
+// everything else 255
+__global__ void select_fill(const int *__restrict__ lab, const int *__restrict__ flag, uint8_t *__restrict__ out,
+                            int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int l = lab[i];
+        out[i] = (l >= 0 && flag[l]) ? 0 : 255;
+    }
+}
+
+// ---- bounding boxes --------------------------------------------------------
+__global__ void bbox_init(int *mnx, int *mxx, int *mny, int *mxy, const int *__restrict__ lab, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (lab[i] == (int)i) {
+            mnx[i] = INT_MAX;
+            mxx[i] = -1;
+            mny[i] = INT_MAX;
+            mxy[i] = -1;
+        }
+    }
+}
+__global__ void bbox_accum(const int *__restrict__ lab, int rows, int cols, int *mnx, int *mxx, int *mny, int *mxy) {
+    int64_t n = (int64_t)rows * cols;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int l = lab[i];
+        if (l < 0) continue;
+        int y = (int)(i / cols), x = (int)(i - (int64_t)y * cols);
+        atomicMin(mnx + l, x);
+        atomicMax(mxx + l, x);
+        atomicMin(mny + l, y);
+        atomicMax(mxy + l, y);
+    }
+}
+__global__ void root_flags(const int *__restrict__ lab, int *__restrict__ f, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        f[i] = lab[i] == (int)i ? 1 : 0;
+}
+__global__ void bbox_write(const int *__restrict__ lab, const int *__restrict__ pos, int64_t n,
+                           const int *__restrict__ total, const int *mnx, const int *mxx, const int *mny,
+                           const int *mxy, int *__restrict__ out, int64_t cap_ints, int *status) {
+    int cnt = *total;
+    if ((int64_t)cnt * 5 > cap_ints) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(status, DEV_QUEUE_FULL);
+        return;
+    }
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (lab[i] != (int)i) continue;
+        int k = pos[i];
+        out[k] = (int)i;
+        out[cnt + k] = mnx[i];
+        out[2 * cnt + k] = mxx[i];
+        out[3 * cnt + k] = mny[i];
+        out[4 * cnt + k] = mxy[i];
+    }
+}
+
+// ---- exclusive scan (three passes) ------------------------------------------
+constexpr int kScanThreads = 1024, kScanItems = 4, kScanTile = kScanThreads * kScanItems;
+
+__device__ int block_exclusive_scan(int v, int *sh, int *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) sh[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0;
+        int z = w;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, z, d);
+            if (lane >= d) z += y;
+        }
+        sh[lane] = z - w;
+        if (lane == 31) sh[32] = z;
+    }
+    __syncthreads();
+    int r = sh[warp] + x - v;
+    if (total) *total = sh[32];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_tiles(const int *__restrict__ in, int *__restrict__ out,
+                                                           int64_t n, int *__restrict__ block_sums) {
+    __shared__ int sh[33];
+    int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+    int v[kScanItems];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = base + k < n ? in[base + k] : 0;
+        s += v[k];
+    }
+    int tot;
+    int pre = block_exclusive_scan(s, sh, &tot);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < n) out[base + k] = pre;
+        pre += v[k];
+    }
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
+}
+__global__ void __launch_bounds__(kScanThreads) scan_sums(int *sums, int nb, int *total) {
+    __shared__ int sh[33];
+    int carry = 0;
+    for (int base = 0; base < nb; base += kScanThreads) {
+        int i = base + threadIdx.x;
+        int v = i < nb ? sums[i] : 0;
+        int tot;
+        int pre = block_exclusive_scan(v, sh, &tot);
+        if (i < nb) sums[i] = pre + carry;
+        carry += tot;
+    }
+    if (threadIdx.x == 0 && total) *total = carry;
+}
+__global__ void scan_add(int *out, int64_t n, const int *__restrict__ sums) {
+    int64_t base = (int64_t)blockIdx.x * kScanTile;
+    int add = sums[blockIdx.x];
+    for (int k = threadIdx.x; k < kScanTile; k += blockDim.x)
+        if (base + k < n) out[base + k] += add;
+}
+
+int blocks(Ctx &c, int64_t n) {
+    int64_t g = (n + kB - 1) / kB;
+    int64_t cap = (int64_t)c.sm_count * 16;
+    return (int)(g < 1 ? 1 : (g < cap ? g : cap));
+}
+
+}  // namespace
+
+int exclusive_scan_i32(Ctx &c, const int32_t *in, int32_t *out, int64_t n, int32_t *d_total, cudaStream_t s) {
+    int nb = (int)((n + kScanTile - 1) / kScanTile);
+    if (nb < 1) nb = 1;
+    scan_tiles<<<nb, kScanThreads, 0, s>>>(in, out, n, c.ws.scan_tmp);
+    scan_sums<<<1, kScanThreads, 0, s>>>(c.ws.scan_tmp, nb, d_total);
+    scan_add<<<nb, 256, 0, s>>>(out, n, c.ws.scan_tmp);
+    NSG_LAUNCH_CHECK(c);
+    return NSG_SUCCESS;
+}
+
+int ccl_u8(Ctx &c, const uint8_t *img, int32_t *parent, int rows, int cols, int conn, int mode, cudaStream_t s) {
+    int64_t n = (int64_t)rows * cols;
+    int g = blocks(c, n);
+    switch (mode) {
+        case CCL_EQUAL:
+            ccl_init<CCL_EQUAL><<<g, kB, 0, s>>>(img, parent, n);
+            ccl_merge<CCL_EQUAL><<<g, kB, 0, s>>>(img, parent, rows, cols, conn);
+            break;
+        case CCL_NONZERO:
+            ccl_init<CCL_NONZERO><<<g, kB, 0, s>>>(img, parent, n);
+            ccl_merge<CCL_NONZERO><<<g, kB, 0, s>>>(img, parent, rows, cols, conn);
+            break;
+        default:
+            ccl_init<CCL_NOT255><<<g, kB, 0, s>>>(img, parent, n);
+            ccl_merge<CCL_NOT255><<<g, kB, 0, s>>>(img, parent, rows, cols, conn);
+            break;
+    }
+    ccl_flatten<<<g, kB, 0, s>>>(parent, n);
+    NSG_LAUNCH_CHECK(c);
+    return NSG_SUCCESS;
+}
+
+int ccl_f32_masked(Ctx &c, const float *val, const uint8_t *valid, int32_t *parent, int rows, int cols, int conn,
+                   cudaStream_t s) {
+    int64_t n = (int64_t)rows * cols;
+    int g = blocks(c, n);
+    cclf_init<<<g, kB, 0, s>>>(valid, parent, n);
+    cclf_merge<<<g, kB, 0, s>>>(val, valid, parent, rows, cols, conn);
+    ccl_flatten<<<g, kB, 0, s>>>(parent, n);
+    NSG_LAUNCH_CHECK(c);
+    return NSG_SUCCESS;
+}
+
+// scratch: i32[0] (labels), i32[1] (areas)
+int bwareaopen_dev(Ctx &c, const uint8_t *img, uint8_t *out, int rows, int cols, int min_size, int max_size,
+                   int conn, int *d_count, cudaStream_t s) {
+    int64_t n = (int64_t)rows * cols;
+    int *lab = c.ws.i32[0], *area = c.ws.i32[1];
+    NSG_TRY(ccl_u8(c, img, lab, rows, cols, conn, CCL_EQUAL, s));
+    NSG_CUDA_TRY(c, cudaMemsetAsync(area, 0, n * sizeof(int), s));
+    NSG_CUDA_TRY(c, cudaMemsetAsync(d_count, 0, sizeof(int), s));
+    int g = blocks(c, n);
+    area_count<<<g, kB, 0, s>>>(lab, area, n);
+    area_select<<<g, kB, 0, s>>>(lab, area, n, min_size, max_size, out, d_count);
+    NSG_LAUNCH_CHECK(c);
+    return NSG_SUCCESS;
+}
+
+// scratch: i32[0] (labels), i32[1] (flags)
+int recon_binary_dev(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t *out, int rows, int cols, int conn,
+                     cudaStream_t s) {
+    int64_t n = (int64_t)rows * cols;
+    int *lab = c.ws.i32[0], *flag = c.ws.i32[1];
+    NSG_TRY(ccl_u8(c, mask, lab, rows, cols, conn, CCL_NONZERO, s));
+    int g = blocks(c, n);
+    zero_flags_at_roots<<<g, kB, 0, s>>>(lab, flag, n);
+    flag_seeds<<<g, kB, 0, s>>>(lab, marker, mask, flag, n);
+    select_recon<<<g, kB, 0, s>>>(lab, flag, marker, mask, out, n);
+    NSG_LAUNCH_CHECK(c);
+    return NSG_SUCCESS;
+}
+
+int bwselect_dev(Ctx &c, const uint8_t *bw, const uint8_t *seeds, uint8_t *out, int rows, int cols, int conn,
+                 cudaStream_t s) {
+    int64_t n = (int64_t)rows * cols;
+    int *lab = c.ws.i32[0], *flag = c.ws.i32[1];
+    NSG_TRY(ccl_u8(c, bw, lab, rows, cols, conn, CCL_NONZERO, s));
+    int g = blocks(c, n);
+    zero_flags_at_roots<<<g, kB, 0, s>>>(lab, flag, n);
+    flag_seeds<<<g, kB, 0, s>>>(lab, seeds, bw, flag, n);
+    select_bw<<<g, kB, 0, s>>>(lab, flag, bw, out, n);
+    NSG_LAUNCH_CHECK(c);
+    return NSG_SUCCESS;
+}
+
+int fill_holes_dev(Ctx &c, const uint8_t *img, uint8_t *out, int rows, int cols, int conn, cudaStream_t s) {
+    int64_t n = (int64_t)rows * cols;
+    int *lab = c.ws.i32[0], *flag = c.ws.i32[1];
+    NSG_TRY(ccl_u8(c, img, lab, rows, cols, conn, CCL_NOT255, s));
+    int g = blocks(c, n);
+    zero_flags_at_roots<<<g, kB, 0, s>>>(lab, flag, n);
+    flag_border<<<blocks(c, 2 * (int64_t)rows + 2 * cols), kB, 0, s>>>(lab, flag, rows, cols);
+    select_fill<<<g, kB, 0, s>>>(lab, flag, out, n);
+    NSG_LAUNCH_CHECK(c);
+    return NSG_SUCCESS;
+}
+
+int bwlabel_dev(Ctx &c, const uint8_t *img, int32_t *labels, int rows, int cols, int conn, cudaStream_t s) {
+    return ccl_u8(c, img, labels, rows, cols, conn, CCL_EQUAL, s);
+}
+
+// scratch: i32[0..4]; d_bbox holds cap_ints ints (5 per component)
+int bbox_dev(Ctx &c, const int32_t *labels, int rows, int cols, int32_t *d_bbox, int64_t cap_ints, int *d_count,
+             cudaStream_t s) {
+    int64_t n = (int64_t)rows * cols;
+    int *mnx = c.ws.i32[0], *mxx = c.ws.i32[1], *mny = c.ws.i32[2], *mxy = c.ws.i32[3], *pos = c.ws.i32[4];
+    int g = blocks(c, n);
+    bbox_init<<<g, kB, 0, s>>>(mnx, mxx, mny, mxy, labels, n);
+    bbox_accum<<<g, kB, 0, s>>>(labels, rows, cols, mnx, mxx, mny, mxy);
+    root_flags<<<g, kB, 0, s>>>(labels, pos, n);
+    NSG_TRY(exclusive_scan_i32(c, pos, pos, n, d_count, s));
+    bbox_write<<<g, kB, 0, s>>>(labels, pos, n, d_count, mnx, mxx, mny, mxy, d_bbox, cap_ints,
+                                c.ws.ctrl + C_STATUS);
+    NSG_LAUNCH_CHECK(c);
+    return NSG_SUCCESS;
+}
+
+}  // namespace nsg

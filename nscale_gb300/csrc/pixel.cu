@@ -1,0 +1,182 @@
+// pixel.cu — the elementwise stages of segmentNuclei, fused where the
+// reference runs them back to back.
+//
+//  * background test + count       HistologicalEntities.cpp:93-109, 123-137
+//  * RBC ratio masks, red invert   HistologicalEntities.cpp:54-71, 158
+//  * diffIm thresholds             HistologicalEntities.cpp:211, 227, 279
+//  * masks / negated distances     HistologicalEntities.cpp:295, 366-374, 407
+#include <float.h>
+
+#include "nsg_internal.cuh"
+
+namespace nsg {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ void warp_add_u64(unsigned long long *dst, unsigned v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(dst, (unsigned long long)v);
+}
+
+// 16 pixels per thread along a row: 48 contiguous bytes of BGR.
+template <int PX>
+__global__ void background_kernel(const uint8_t *__restrict__ bgr, int64_t stride, int rows, int cols, int blue,
+                                  int green, int red, uint8_t *__restrict__ mask,
+                                  unsigned long long *__restrict__ count) {
+    int64_t chunks_per_row = (cols + PX - 1) / PX;
+    int64_t total = chunks_per_row * rows;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t - threadIdx.x < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        unsigned cnt = 0;
+        if (t < total) {
+            int y = (int)(t / chunks_per_row);
+            int x0 = (int)(t - (int64_t)y * chunks_per_row) * PX;
+            const uint8_t *row = bgr + (int64_t)y * stride;
+#pragma unroll
+            for (int k = 0; k < PX; ++k) {
+                int x = x0 + k;
+                if (x < cols) {
+                    const uint8_t *p = row + 3 * x;
+                    bool on = p[0] > blue && p[1] > green && p[2] > red;
+                    cnt += on;
+                    if (mask) mask[(int64_t)y * cols + x] = on ? 255 : 0;
+                }
+            }
+        }
+        warp_add_u64(count, cnt);
+    }
+}
+
+// getRBC's float32 ratios and the red-channel complement in one pass.
+__global__ void front_rbc_kernel(const uint8_t *__restrict__ bgr, int64_t stride, int rows, int cols, float t1,
+                                 float t2, uint8_t *__restrict__ rc, uint8_t *__restrict__ bw1,
+                                 uint8_t *__restrict__ bw2, uint8_t *__restrict__ r2b, int *__restrict__ bw1_count) {
+    int64_t n = (int64_t)rows * cols;
+    for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = i0 + threadIdx.x;
+        unsigned on1 = 0;
+        if (i < n) {
+            int y = (int)(i / cols), x = (int)(i - (int64_t)y * cols);
+            const uint8_t *p = bgr + (int64_t)y * stride + 3 * x;
+            uint8_t B = p[0], G = p[1], R = p[2];
+            // convertTo(CV_32F, 1.0, FLT_EPSILON) on B and G, plain convert on R
+            float bd = __fadd_rn((float)B, FLT_EPSILON);
+            float gd = __fadd_rn((float)G, FLT_EPSILON);
+            float rd = (float)R;
+            float r2g = __fdiv_rn(rd, gd);
+            float rb = __fdiv_rn(rd, bd);
+            on1 = r2g > t1;
+            bw1[i] = on1 ? 255 : 0;
+            bw2[i] = r2g > t2 ? 255 : 0;
+            r2b[i] = rb > 1.0f ? 255 : 0;
+            rc[i] = (uint8_t)(255 - R);
+        }
+        unsigned b = __ballot_sync(0xffffffffu, on1);
+        if ((threadIdx.x & 31) == 0 && b) atomicAdd(bw1_count, __popc(b));
+    }
+}
+
+__global__ void diff_threshold_kernel(const uint8_t *__restrict__ rc, const uint8_t *__restrict__ rec, int64_t n,
+                                      int g1, int g2, uint8_t *__restrict__ o1, uint8_t *__restrict__ o2) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int a = rc[i], b = rec[i];
+        int d = a > b ? a - b : 0;  // saturating u8 subtraction (HE:211)
+        if (o1) o1[i] = d > g1 ? 255 : 0;
+        if (o2) o2[i] = d > g2 ? 255 : 0;
+    }
+}
+
+__global__ void and_not_kernel(uint8_t *__restrict__ io, const uint8_t *__restrict__ nm, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (nm[i]) io[i] = 0;
+}
+
+__global__ void mask_copy_bgr_kernel(const uint8_t *__restrict__ bgr, int64_t stride, const uint8_t *__restrict__ m,
+                                     int rows, int cols, uint8_t *__restrict__ out) {
+    int64_t n = (int64_t)rows * cols;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int y = (int)(i / cols), x = (int)(i - (int64_t)y * cols);
+        const uint8_t *p = bgr + (int64_t)y * stride + 3 * x;
+        bool on = m[i] != 0;
+        out[3 * i + 0] = on ? p[0] : 0;
+        out[3 * i + 1] = on ? p[1] : 0;
+        out[3 * i + 2] = on ? p[2] : 0;
+    }
+}
+
+__global__ void neg_dist_mask_kernel(const float *__restrict__ d, const uint8_t *__restrict__ m, int64_t n,
+                                     float *__restrict__ out) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = m[i] ? -d[i] : -FLT_MAX;
+}
+
+__global__ void invert_kernel(const uint8_t *__restrict__ in, uint8_t *__restrict__ out, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (uint8_t)(255 - in[i]);
+}
+
+}  // namespace
+
+static int blocks_for(Ctx &c, int64_t n) {
+    int64_t want = (n + kBlock - 1) / kBlock;
+    int64_t cap = (int64_t)c.sm_count * 16;
+    return (int)(want < cap ? (want < 1 ? 1 : want) : cap);
+}
+
+int background_count(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int cols, int blue, int green, int red,
+                     uint8_t *mask, int64_t *d_count, cudaStream_t s) {
+    NSG_CUDA_TRY(c, cudaMemsetAsync(d_count, 0, sizeof(int64_t), s));
+    int64_t chunks = (int64_t)((cols + 15) / 16) * rows;
+    background_kernel<16><<<blocks_for(c, chunks), kBlock, 0, s>>>(bgr, stride, rows, cols, blue, green, red, mask,
+                                                                   (unsigned long long *)d_count);
+    NSG_LAUNCH_CHECK(c);
+    return NSG_SUCCESS;
+}
+
+int front_rbc(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int cols, double T1, double T2, uint8_t *rc,
+              uint8_t *bw1, uint8_t *bw2, uint8_t *r2b, int *d_bw1_count, cudaStream_t s) {
+    NSG_CUDA_TRY(c, cudaMemsetAsync(d_bw1_count, 0, sizeof(int), s));
+    int64_t n = (int64_t)rows * cols;
+    front_rbc_kernel<<<blocks_for(c, n), kBlock, 0, s>>>(bgr, stride, rows, cols, (float)T1, (float)T2, rc, bw1, bw2,
+                                                         r2b, d_bw1_count);
+    NSG_LAUNCH_CHECK(c);
+    return NSG_SUCCESS;
+}
+
+int diff_threshold(Ctx &c, const uint8_t *rc, const uint8_t *rec, int rows, int cols, int G1, int G2, uint8_t *o1,
+                   uint8_t *o2, cudaStream_t s) {
+    int64_t n = (int64_t)rows * cols;
+    diff_threshold_kernel<<<blocks_for(c, n), kBlock, 0, s>>>(rc, rec, n, G1, G2, o1, o2);
+    NSG_LAUNCH_CHECK(c);
+    return NSG_SUCCESS;
+}
+
+int and_not(Ctx &c, uint8_t *io, const uint8_t *nm, int64_t n, cudaStream_t s) {
+    and_not_kernel<<<blocks_for(c, n), kBlock, 0, s>>>(io, nm, n);
+    NSG_LAUNCH_CHECK(c);
+    return NSG_SUCCESS;
+}
+
+int mask_copy_bgr(Ctx &c, const uint8_t *bgr, int64_t stride, const uint8_t *m, int rows, int cols, uint8_t *out,
+                  cudaStream_t s) {
+    int64_t n = (int64_t)rows * cols;
+    mask_copy_bgr_kernel<<<blocks_for(c, n), kBlock, 0, s>>>(bgr, stride, m, rows, cols, out);
+    NSG_LAUNCH_CHECK(c);
+    return NSG_SUCCESS;
+}
+
+int neg_dist_mask(Ctx &c, const float *d, const uint8_t *m, int64_t n, float *out, cudaStream_t s) {
+    neg_dist_mask_kernel<<<blocks_for(c, n), kBlock, 0, s>>>(d, m, n, out);
+    NSG_LAUNCH_CHECK(c);
+    return NSG_SUCCESS;
+}
+
+int invert_u8_dev(Ctx &c, const uint8_t *in, uint8_t *out, int64_t n, cudaStream_t s) {
+    invert_kernel<<<blocks_for(c, n), kBlock, 0, s>>>(in, out, n);
+    NSG_LAUNCH_CHECK(c);
+    return NSG_SUCCESS;
+}
+
+}  // namespace nsg

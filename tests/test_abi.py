@@ -1,0 +1,49 @@
+"""CPU tests of the C ABI: libnsg.so builds, loads without a GPU, and exports
+every function include/nsg.h declares."""
+import os
+import re
+import subprocess
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared() -> set[str]:
+    src = open(os.path.join(ROOT, "include", "nsg.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return set(re.findall(r"\b(nsg_[a-z0-9_]+)\s*\(", src))
+
+
+def test_header_functions_are_exported(nsg):
+    from nscale_gb300 import _lib
+    names = declared()
+    assert len(names) >= 25
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (nsg_[a-z0-9_]+)", out))
+    missing = names - exported
+    assert not missing, f"declared but not exported: {sorted(missing)}"
+    bound = set(_lib.exported_symbols())
+    assert names <= bound, f"not bound in _lib: {sorted(names - bound)}"
+
+
+def test_host_only_calls(nsg):
+    import ctypes as C
+    from nscale_gb300 import _lib
+    assert nsg.nsg_version() >= 10000
+    p = _lib.SegParams()
+    nsg.nsg_default_params(C.byref(p))
+    assert (p.blue, p.green, p.red, p.T1, p.T2, p.G1, p.minSize, p.maxSize, p.G2, p.minSizePl, p.minSizeSeg,
+            p.maxSizeSeg, p.fillHolesConnectivity, p.reconConnectivity, p.watershedConnectivity) == \
+        (220, 220, 220, 5.0, 4.0, 80, 11, 1000, 45, 30, 21, 1000, 4, 8, 8)
+    assert nsg.nsg_status_string(3) == b"NO_CANDIDATES_LEFT"
+    assert nsg.nsg_status_string(-12) == b"ERR_TIMEOUT"
+    # argument errors are reported without touching a device
+    assert nsg.nsg_context_create(None, 10, 10, 0) == _lib.ERR_ARG
+    assert nsg.nsg_context_destroy(None) == _lib.ERR_ARG
+
+
+def test_product_does_not_link_the_oracle(nsg):
+    from nscale_gb300 import _lib
+    out = subprocess.run(["nm", "-D", _lib.LIB_PATH], capture_output=True, text=True).stdout
+    assert "orc_" not in out and "ref_cc_" not in out
+    deps = subprocess.run(["ldd", _lib.LIB_PATH], capture_output=True, text=True).stdout
+    assert "oracle" not in deps and "torch" not in deps

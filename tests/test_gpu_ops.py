@@ -1,0 +1,209 @@
+"""GPU parity tests: every operation on the segmentNuclei path, called through
+libnsg.so (the C ABI), against the oracle on the same seeded inputs.
+Integer, byte and label outputs must be bit-exact; float32 outputs must be
+equal as values (IEEE ==, so +0 and -0 compare equal)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(1, 1), (1, 37), (41, 1), (64, 64), (97, 131), (256, 300)]
+
+
+def T(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def N(t):
+    import torch
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def masks(rows, cols, seed):
+    from nscale_gb300 import synth
+    yield "discs", synth.disc_mask(rows, cols, seed=seed)
+    yield "zeros", np.zeros((rows, cols), np.uint8)
+    yield "ones", np.full((rows, cols), 255, np.uint8)
+    rng = np.random.default_rng(seed)
+    yield "noise", ((rng.random((rows, cols)) < 0.5) * 255).astype(np.uint8)
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_background_and_rbc(cuda, orc, shape):
+    from nscale_gb300 import synth
+    from nscale_gb300.histological_entities import HistologicalEntities as HE
+    img = synth.he_tile(*shape, seed=0x5EED2000 + shape[0])
+    m, n = HE.getBackground(T(img))
+    om, on = orc.get_background(img)
+    assert n == on
+    np.testing.assert_array_equal(N(m), om)
+    np.testing.assert_array_equal(N(HE.getRBC(T(img))), orc.get_rbc(img))
+
+
+def test_rbc_on_threshold_colour(cuda, orc):
+    """RBC colour (200, 40, 40) puts R/G exactly at T1 = 5; a T1 ramp around it."""
+    from nscale_gb300.histological_entities import HistologicalEntities as HE
+    img = np.zeros((16, 256, 3), np.uint8)
+    img[..., 0] = np.arange(256)[None, :]          # B ramp
+    img[..., 1] = np.arange(16)[:, None] * 4 + 38  # G around 40
+    img[..., 2] = 200
+    for t1, t2 in ((5.0, 4.0), (2.5, 2.0), (5.1, 4.9)):
+        np.testing.assert_array_equal(N(HE.getRBC(T(img), t1, t2)), orc.get_rbc(img, t1, t2))
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_morph_open(cuda, orc, shape):
+    from nscale_gb300 import morphologic_operations as MO
+    rng = np.random.default_rng(shape[0] * 7 + shape[1])
+    img = rng.integers(0, 256, size=shape).astype(np.uint8)
+    for se in (MO.disk19().numpy(), MO.cross3().numpy(), np.ones((5, 5), np.uint8),
+               np.array([[1, 0, 0], [0, 1, 0], [1, 0, 1]], np.uint8)):
+        np.testing.assert_array_equal(N(MO.erode(T(img), se)), orc.erode(img, se))
+        np.testing.assert_array_equal(N(MO.dilate(T(img), se)), orc.dilate(img, se))
+        np.testing.assert_array_equal(N(MO.morphOpen(T(img), se)), orc.morph_open(img, se))
+
+
+@pytest.mark.parametrize("shape", SHAPES + [(1024, 1024), (513, 1999)])
+@pytest.mark.parametrize("conn", [4, 8])
+def test_imreconstruct_u8(cuda, orc, shape, conn):
+    from nscale_gb300 import morphologic_operations as MO
+    from nscale_gb300 import synth
+    marker, mask = synth.recon_inputs(*shape, seed=0x5EED0001 + shape[1])
+    np.testing.assert_array_equal(N(MO.imreconstruct(T(marker), T(mask), conn)),
+                                  orc.imreconstruct(marker, mask, conn))
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (37, 1), (64, 64), (97, 131), (600, 700)])
+@pytest.mark.parametrize("conn", [4, 8])
+def test_imreconstruct_f32(cuda, orc, shape, conn):
+    from nscale_gb300 import morphologic_operations as MO
+    from nscale_gb300 import synth
+    marker, mask = synth.recon_inputs_f32(*shape, seed=0x5EED0011 + shape[0])
+    # signed values exercise the zero ring
+    marker = marker - np.float32(100.0)
+    mask = mask - np.float32(50.0)
+    got = N(MO.imreconstruct(T(marker), T(mask), conn))
+    ref = orc.imreconstruct(marker, mask, conn)
+    assert (got == ref).all()
+
+
+def test_imreconstruct_timeout_is_reported(cuda):
+    """A spin budget of one iteration makes the persistent kernel give up: the
+    call returns NSG_ERR_TIMEOUT and the context stays usable."""
+    from nscale_gb300 import _lib, morphologic_operations as MO
+    from nscale_gb300 import synth
+    from nscale_gb300.context import get_context
+    marker, mask = synth.recon_inputs(512, 512, seed=3)
+    ctx = get_context(512, 512)
+    ctx.set_spin_budget(1)
+    try:
+        with pytest.raises(_lib.NsgError) as e:
+            for _ in range(50):
+                MO.imreconstruct(T(marker), T(mask), 8)
+        assert e.value.code == _lib.ERR_TIMEOUT
+    finally:
+        ctx.set_spin_budget(0)
+    out = MO.imreconstruct(T(marker), T(mask), 8)
+    assert N(out).shape == (512, 512)
+
+
+@pytest.mark.parametrize("shape", SHAPES + [(1024, 1024)])
+@pytest.mark.parametrize("conn", [4, 8])
+def test_binary_ops(cuda, orc, shape, conn):
+    from nscale_gb300 import morphologic_operations as MO
+    for name, m in masks(*shape, seed=0x5EED3000 + shape[0]):
+        np.testing.assert_array_equal(N(MO.imfillHoles(T(m), True, conn)), orc.imfill_holes(m, conn), err_msg=name)
+        seeds = np.zeros_like(m)
+        seeds[::7, ::5] = 255
+        np.testing.assert_array_equal(N(MO.bwselect(T(m), T(seeds), conn)), orc.bwselect(m, seeds, conn),
+                                      err_msg=name)
+        marker = (m & seeds)
+        np.testing.assert_array_equal(N(MO.imreconstructBinary(T(marker), T(m), conn)),
+                                      orc.imreconstruct_binary(marker, m, conn), err_msg=name)
+
+
+@pytest.mark.parametrize("shape", SHAPES + [(1024, 1024), (2048, 777)])
+@pytest.mark.parametrize("conn", [4, 8])
+def test_bwlabel_and_areaopen(cuda, orc, shape, conn):
+    from nscale_gb300 import morphologic_operations as MO
+    for name, m in masks(*shape, seed=0x5EED4000 + shape[1]):
+        np.testing.assert_array_equal(N(MO.bwlabel2(T(m), conn)), orc.bwlabel2(m, conn), err_msg=name)
+        for lo, hi in ((11, 1000), (21, 1000), (30, 2 ** 31 - 1), (1, 3)):
+            out, n = MO.bwareaopen2(T(m), False, True, lo, hi, conn)
+            oout, on = orc.bwareaopen2(m, lo, hi, conn)
+            assert n == on, (name, lo, hi)
+            np.testing.assert_array_equal(N(out), oout, err_msg=name)
+    rng = np.random.default_rng(5)
+    mv = (rng.integers(0, 4, size=shape) * 60).astype(np.uint8)  # equal-value components
+    np.testing.assert_array_equal(N(MO.bwlabel2(T(mv), conn)), orc.bwlabel2(mv, conn))
+
+
+def test_bwlabel_matches_reference_golden(cuda):
+    """GPU labels against the reference's own ConnComponents outputs."""
+    import os
+    from nscale_gb300 import morphologic_operations as MO
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "cc_golden.npz"))
+    for name in sorted({k.split("/")[0] for k in g.files}):
+        img = g[f"{name}/img"]
+        for conn in (4, 8):
+            np.testing.assert_array_equal(N(MO.bwlabel2(T(img), conn)), g[f"{name}/label{conn}"], err_msg=name)
+
+
+@pytest.mark.parametrize("shape", SHAPES + [(1024, 1024)])
+def test_bounding_box(cuda, orc, shape):
+    import ctypes as C
+    from nscale_gb300 import morphologic_operations as MO
+    from nscale_gb300.context import get_context, ptr, stream_handle
+    for name, m in masks(*shape, seed=0x5EED5000 + shape[0]):
+        lab = MO.bwlabel2(T(m), 8)
+        ctx = get_context(*shape)
+        cap = shape[0] * shape[1]
+        buf = np.zeros(5 * cap + 5, np.int32)
+        cnt = C.c_int(0)
+        ctx.check(ctx.L.nsg_bounding_box(ctx.h, ptr(lab), shape[0], shape[1], buf.ctypes.data, cap, C.byref(cnt),
+                                         stream_handle()))
+        n = cnt.value
+        np.testing.assert_array_equal(buf[:5 * n].reshape(5, n), orc.bounding_box(N(lab)), err_msg=name)
+
+
+@pytest.mark.parametrize("shape", SHAPES + [(1024, 1024), (700, 1500)])
+def test_dist_transform(cuda, orc, shape):
+    from nscale_gb300 import morphologic_operations as MO
+    from nscale_gb300 import synth
+    for m in (synth.disc_pairs_mask(*shape, seed=0x5EED0002), np.full(shape, 255, np.uint8),
+              np.zeros(shape, np.uint8)):
+        np.testing.assert_array_equal(N(MO.distTransform(T(m))), orc.dist_transform(m))
+
+
+def _distance2_inputs(shape, seed):
+    from nscale_gb300 import synth
+    m = synth.disc_pairs_mask(*shape, seed=seed)
+    d = np.asarray(__import__("oracle").dist_transform(m))
+    distance = np.where(m > 0, -d, -np.finfo(np.float32).max).astype(np.float32)
+    return m, distance
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (64, 64), (97, 131), (512, 512)])
+def test_imhmin_and_minima(cuda, orc, shape):
+    from nscale_gb300 import morphologic_operations as MO
+    m, distance = _distance2_inputs(shape, 0x5EED0002 + shape[0])
+    d2 = N(MO.imhmin(T(distance), 1.0, 8))
+    od2 = orc.imhmin(distance, 1.0, 8)
+    assert (d2 == od2).all()
+    for conn in (4, 8):
+        np.testing.assert_array_equal(N(MO.localMinima(T(od2), conn)), orc.local_minima(od2, conn))
+        np.testing.assert_array_equal(N(MO.localMaxima(T(-od2), conn)), orc.local_maxima(-od2, conn))
+
+
+@pytest.mark.parametrize("shape", [(3, 3), (64, 64), (97, 131), (256, 300)])
+@pytest.mark.parametrize("conn", [4, 8])
+def test_watershed2(cuda, orc, shape, conn):
+    from nscale_gb300 import morphologic_operations as MO
+    from nscale_gb300 import synth
+    m, distance = _distance2_inputs(shape, 0x5EED0022 + shape[1])
+    d2 = orc.imhmin(distance, 1.0, 8)
+    bgr = synth.colorize_mask(m, seed=0x5EED0000)
+    got = N(MO.watershed2(T(bgr), T(d2), conn))
+    np.testing.assert_array_equal(got, orc.watershed2(bgr, d2, conn))

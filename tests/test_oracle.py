@@ -1,0 +1,179 @@
+"""CPU tests of the oracle (the checker): pinned against the reference's own
+ConnComponents outputs (tests/golden/cc_golden.npz, generated by
+tests/golden/make_golden.py from src/segment/ConnComponents.cpp), against
+independent scipy implementations, and on known-answer cases."""
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+INT_MAX = 2 ** 31 - 1
+
+
+@pytest.fixture(scope="module")
+def cc_gold():
+    return np.load(os.path.join(GOLD, "cc_golden.npz"))
+
+
+def _names(g):
+    return sorted({k.split("/")[0] for k in g.files})
+
+
+def test_cc_label_matches_reference(orc, cc_gold):
+    for name in _names(cc_gold):
+        img = cc_gold[f"{name}/img"]
+        for conn in (4, 8):
+            got = orc.cc_label(img, conn)
+            np.testing.assert_array_equal(got, cc_gold[f"{name}/label{conn}"], err_msg=f"{name} conn {conn}")
+
+
+def test_area_threshold_matches_reference(orc, cc_gold):
+    for name in _names(cc_gold):
+        for conn in (4, 8):
+            lab = cc_gold[f"{name}/label{conn}"]
+            for lo, hi in ((11, 1000), (21, 1000), (30, INT_MAX), (1, 5)):
+                got, n = orc.area_threshold_labeled(lab, lo, hi)
+                np.testing.assert_array_equal(got, cc_gold[f"{name}/athr{conn}_{lo}_{hi}"])
+                assert n == int(cc_gold[f"{name}/athr{conn}_{lo}_{hi}_n"]), (name, conn, lo, hi)
+
+
+def test_bwareaopen_matches_reference_area_threshold(orc, cc_gold):
+    """ConnComponents::areaThreshold (one-pass form) and bwareaopen2 agree."""
+    for name in _names(cc_gold):
+        img = cc_gold[f"{name}/img"]
+        for conn in (4, 8):
+            ref = cc_gold[f"{name}/areathr{conn}"]
+            out, n = orc.bwareaopen2(img, 11, 1000, conn)
+            np.testing.assert_array_equal(out, np.where(ref > -1, 255, 0).astype(np.uint8), err_msg=name)
+            assert n == int(cc_gold[f"{name}/areathr{conn}_n"])
+
+
+def test_bounding_box_matches_reference(orc, cc_gold):
+    for name in _names(cc_gold):
+        for conn in (4, 8):
+            lab = cc_gold[f"{name}/label{conn}"]
+            # bug-compatible restatement: the reference stops at a 0 or -1 label
+            np.testing.assert_array_equal(orc.bounding_box_refbug(lab, -1), cc_gold[f"{name}/bbox{conn}"])
+            np.testing.assert_array_equal(orc.bounding_box_refbug(lab, 0), cc_gold[f"{name}/bbox{conn}_bg0"])
+            # where the reference's scan is not cut short, the correct boxes agree with it
+            if not (lab == 0).any():
+                np.testing.assert_array_equal(orc.bounding_box(lab), cc_gold[f"{name}/bbox{conn}"])
+
+
+def _canon(lab):
+    """relabel any labelling to min-raster-index labels (-1 background)."""
+    flat = lab.ravel()
+    out = np.full(flat.shape, -1, np.int64)
+    fg = flat > 0 if lab.min() >= 0 else flat >= 0
+    ids = flat[fg]
+    idx = np.nonzero(fg)[0]
+    first = {}
+    for l, i in zip(ids.tolist(), idx.tolist()):
+        if l not in first:
+            first[l] = i
+    out[fg] = [first[l] for l in ids.tolist()]
+    return out.reshape(lab.shape)
+
+
+def test_cc_label_matches_scipy(orc):
+    ndi = pytest.importorskip("scipy.ndimage")
+    from nscale_gb300 import synth
+    m = synth.disc_mask(200, 173, seed=0x5EED0201)
+    for conn, st in ((4, ndi.generate_binary_structure(2, 1)), (8, ndi.generate_binary_structure(2, 2))):
+        lab, _ = ndi.label(m > 0, structure=st)
+        np.testing.assert_array_equal(orc.bwlabel2(m, conn), _canon(lab))
+
+
+def test_edt_matches_scipy(orc):
+    ndi = pytest.importorskip("scipy.ndimage")
+    from nscale_gb300 import synth
+    m = synth.disc_pairs_mask(300, 277, seed=0x5EED0202)
+    ref = ndi.distance_transform_edt(m > 0).astype(np.float32)
+    np.testing.assert_array_equal(orc.dist_transform(m), ref)
+
+
+def test_edt_no_zero_pixel(orc):
+    m = np.full((7, 9), 255, np.uint8)
+    np.testing.assert_array_equal(orc.dist_transform(m), np.full((7, 9), np.sqrt(np.float32(1e15)), np.float32))
+
+
+def test_fill_holes_matches_scipy(orc):
+    ndi = pytest.importorskip("scipy.ndimage")
+    from nscale_gb300 import synth
+    m = synth.disc_mask(211, 190, seed=0x5EED0203)
+    for conn, st in ((4, ndi.generate_binary_structure(2, 1)), (8, ndi.generate_binary_structure(2, 2))):
+        ref = ndi.binary_fill_holes(m > 0, structure=st)
+        np.testing.assert_array_equal(orc.imfill_holes(m, conn), np.where(ref, 255, 0).astype(np.uint8))
+
+
+def test_recon_known_answer(orc):
+    # 1-D profile: a marker spike reconstructs the whole plateau under the mask
+    mask = np.array([[0, 5, 9, 9, 3, 7, 7, 7, 2, 8]], np.uint8)
+    marker = np.array([[0, 0, 0, 9, 0, 0, 0, 0, 0, 0]], np.uint8)
+    out = orc.imreconstruct(marker, mask, 4)
+    np.testing.assert_array_equal(out, [[0, 5, 9, 9, 3, 3, 3, 3, 2, 2]])
+    # float with a negative marker next to the zero ring: the ring propagates 0
+    maskf = np.array([[2.0, 2.0, 2.0]], np.float32)
+    markerf = np.array([[-1.0, -1.0, -1.0]], np.float32)
+    np.testing.assert_array_equal(orc.imreconstruct(markerf, maskf, 4), [[0.0, 0.0, 0.0]])
+
+
+def test_recon_matches_naive_fixed_point(orc):
+    """reconstruction == iterated geodesic dilation on the 0-padded image."""
+    from nscale_gb300 import synth
+    marker, mask = synth.recon_inputs(40, 37, seed=0x5EED0204)
+    for conn in (4, 8):
+        got = orc.imreconstruct(marker, mask, conn)
+        cur = np.minimum(marker, mask).astype(np.int32)
+        while True:
+            p = np.pad(cur, 1)
+            nb = [p[1:-1, 1:-1], p[:-2, 1:-1], p[2:, 1:-1], p[1:-1, :-2], p[1:-1, 2:]]
+            if conn == 8:
+                nb += [p[:-2, :-2], p[:-2, 2:], p[2:, :-2], p[2:, 2:]]
+            nxt = np.maximum(cur, np.minimum(np.max(nb, axis=0), mask))
+            if (nxt == cur).all():
+                break
+            cur = nxt
+        np.testing.assert_array_equal(got, cur.astype(np.uint8))
+
+
+def test_local_maxima_plateaus(orc):
+    img = np.array([[1, 1, 1, 0],
+                    [1, 3, 3, 0],
+                    [1, 3, 2, 0],
+                    [0, 1, 1, 5]], np.float32)
+    out = orc.local_maxima(img, 8)
+    exp = np.zeros((4, 4), np.uint8)
+    exp[1, 1] = exp[1, 2] = exp[2, 1] = 255  # the 3-plateau
+    exp[3, 3] = 255                           # the 5 peak
+    np.testing.assert_array_equal(out, exp)
+
+
+def test_watershed_two_markers_line(orc):
+    """Two flat basins split by a line where their floods meet."""
+    rows, cols = 5, 9
+    img = np.zeros((rows, cols, 3), np.uint8)
+    img[:, :, :] = 100
+    markers = np.zeros((rows, cols), np.int32)
+    markers[2, 1] = 1
+    markers[2, 7] = 2
+    out = orc.cv_watershed(img, markers)
+    assert (out[0, :] == -1).all() and (out[-1, :] == -1).all()
+    assert (out[1:-1, 1:4] == 1).all() and (out[1:-1, 5:8] == 2).all()
+    assert (out[1:-1, 4] == -1).all()
+
+
+def test_segment_small_regression(orc):
+    g = np.load(os.path.join(GOLD, "seg_small.npz"))
+    for key in ("tile_a", "tile_b"):
+        st, lab, _, bbox, _ = orc.segment_nuclei(g[f"{key}/img"])
+        assert st == int(g[f"{key}/status"])
+        np.testing.assert_array_equal(lab, g[f"{key}/labels"])
+        np.testing.assert_array_equal(bbox, g[f"{key}/bbox"])
+
+
+def test_segment_background_status(orc):
+    from nscale_gb300 import synth
+    st, lab, _, bbox, _ = orc.segment_nuclei(synth.white_tile(64, 80, seed=1))
+    assert st == 1 and (lab == -1).all() and bbox.shape == (5, 0)
