@@ -146,6 +146,16 @@ int nsg_local_minima_f32(nsg_context *ctx, const float *img, uint8_t *out, int r
  * watershed lines. */
 int nsg_watershed(nsg_context *ctx, const uint8_t *bgr, const float *img, int32_t *labels_out, int rows, int cols,
                   int conn, nsg_stream_t stream);
+/* The same watershed2 with the flood run by the reference's serial queue
+ * discipline on one GPU thread (no counterpart of its own in the reference:
+ * it is the verified fallback of nsg_watershed, exposed for cross-checks). */
+int nsg_watershed_serial(nsg_context *ctx, const uint8_t *bgr, const float *img, int32_t *labels_out, int rows,
+                         int cols, int conn, nsg_stream_t stream);
+/* Diagnostics of the last nsg_watershed / segmentNuclei flood (16 ints):
+ * [0] fallback code (0 = domain-parallel path taken), [1] flood domains,
+ * [2] background entries recorded, [6] level of the first background pop,
+ * [9] 1 if a background flood event happened, [11] BFS layers. */
+int nsg_watershed_diagnostics(nsg_context *ctx, int *out16, nsg_stream_t stream);
 /* ConnComponents::boundingBox (ConnComponents.cpp:241-284) on a -1-background
  * label image: writes compcount entries of (label, minx, maxx, miny, maxy) as
  * five consecutive int32 arrays into HOST memory `bbox_out` (capacity

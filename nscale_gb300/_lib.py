@@ -72,6 +72,8 @@ _SIGS = {
     "nsg_local_maxima_f32": (_I, [_P, _P, _P, _I, _I, _I, _P]),
     "nsg_local_minima_f32": (_I, [_P, _P, _P, _I, _I, _I, _P]),
     "nsg_watershed": (_I, [_P, _P, _P, _P, _I, _I, _I, _P]),
+    "nsg_watershed_serial": (_I, [_P, _P, _P, _P, _I, _I, _I, _P]),
+    "nsg_watershed_diagnostics": (_I, [_P, _P, _P]),
     "nsg_bounding_box": (_I, [_P, _P, _I, _I, _P, _I, C.POINTER(_I), _P]),
     "nsg_segment_nuclei": (_I, [_P, _P, _I, _I, C.c_size_t, C.POINTER(SegParams), _P, _P, C.POINTER(_I),
                                 C.POINTER(C.POINTER(C.c_int32)), _P]),

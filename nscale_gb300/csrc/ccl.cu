@@ -93,9 +93,19 @@ __global__ void ccl_merge(const uint8_t *__restrict__ img, int *parent, int rows
     }
 }
 
+// Final pass: every pixel points at its root.  The find here must not
+// compress paths: a compressing find could overwrite another pixel's final
+// root with an intermediate ancestor after that pixel was written.
 __global__ void ccl_flatten(int *parent, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        if (__ldcg(parent + i) >= 0) parent[i] = find_root(parent, (int)i);
+        int x = __ldcg(parent + i);
+        if (x < 0) continue;
+        for (;;) {
+            int p = __ldcg(parent + x);
+            if (p == x) break;
+            x = p;
+        }
+        parent[i] = x;
     }
 }
 

@@ -102,6 +102,7 @@ int nsg_context_create(nsg_context **out, int max_rows, int max_cols, int device
     sizes[ns++] = al(kCtrlInts * 4);         // ctrl
     sizes[ns++] = al(64 * 8);                // ctr64
     sizes[ns++] = al((P / 256 + 1024) * 4);  // scan_tmp
+    sizes[ns++] = al(pws_workspace_bytes((int64_t)P));  // watershed workspace
     size_t total = 0;
     for (int i = 0; i < ns; ++i) total += sizes[i];
     char *base = nullptr;
@@ -129,6 +130,8 @@ int nsg_context_create(nsg_context **out, int max_rows, int max_cols, int device
     c.ws.ctrl = (int *)take();
     c.ws.ctr64 = (int64_t *)take();
     c.ws.scan_tmp = (int32_t *)take();
+    c.ws.wsb_bytes = sizes[k];
+    c.ws.wsb = take();
     if (cudaMallocHost((void **)&c.ws.h_ctrl, kCtrlInts * 4) != cudaSuccess ||
         cudaMallocHost((void **)&c.ws.h_ctr64, 64 * 8) != cudaSuccess) {
         cudaGetLastError();

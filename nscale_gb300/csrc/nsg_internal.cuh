@@ -39,6 +39,9 @@ struct Workspace {
     int64_t *ctr64 = nullptr;  // device 64-bit counters
     int64_t *h_ctr64 = nullptr;
     int32_t *scan_tmp = nullptr;  // block sums for scans
+    // watershed workspace (carved per call by watershed_dev)
+    char *wsb = nullptr;
+    size_t wsb_bytes = 0;
 };
 
 constexpr int kCtrlInts = 4096;
@@ -184,5 +187,16 @@ int local_extrema_dev(Ctx &c, const float *img, uint8_t *out, int rows, int cols
 // watershed.cu (uses i32[2..4], u8[0..2])
 int watershed_dev(Ctx &c, const uint8_t *bgr, const float *img, int32_t *out, int rows, int cols, int conn,
                   cudaStream_t s);
+// watershed_pws.cu: domain-parallel exact Meyer flooding of a padded marker
+// image (markers > 0, unknown 0, negative reset to 0) with packed BGR colours.
+// Writes the flooded labels into outp (padded); falls back to the serial
+// flood on the device when its exactness conditions do not hold.
+size_t pws_workspace_bytes(int64_t npad);
+int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int W, cudaStream_t s);
+int ws_flood_serial_launch(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int W, bool conditional,
+                           cudaStream_t s);
+int watershed_serial_dev(Ctx &c, const uint8_t *bgr, const float *img, int32_t *out, int rows, int cols, int conn,
+                         cudaStream_t s);
+int watershed_diag(Ctx &c, int *out16, cudaStream_t s);
 
 }  // namespace nsg

@@ -382,6 +382,21 @@ int nsg_watershed(nsg_context *h, const uint8_t *bgr, const float *img, int32_t 
     });
 }
 
+int nsg_watershed_serial(nsg_context *h, const uint8_t *bgr, const float *img, int32_t *labels_out, int rows,
+                         int cols, int conn, nsg_stream_t s) {
+    return run_op(h, s, [&](Ctx &c) {
+        NSG_TRY(check_dims(c, rows, cols));
+        NSG_TRY(check_conn(c, conn));
+        if (!bgr || !img || !labels_out) return NSG_ERR_ARG;
+        return watershed_serial_dev(c, bgr, img, labels_out, rows, cols, conn, S(s));
+    });
+}
+
+int nsg_watershed_diagnostics(nsg_context *h, int *out16, nsg_stream_t s) {
+    if (!h || !out16) return NSG_ERR_ARG;
+    return watershed_diag(h->c, out16, S(s));
+}
+
 int nsg_bounding_box(nsg_context *h, const int32_t *labels, int rows, int cols, int32_t *bbox_out, int capacity,
                      int *compcount, nsg_stream_t s) {
     int r = run_op(h, s, [&](Ctx &c) {

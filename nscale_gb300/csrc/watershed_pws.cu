@@ -1,0 +1,1267 @@
+// watershed_pws.cu — exact, domain-parallel reproduction of OpenCV's Meyer
+// flooding order (cv::watershed as nscale::watershed2 calls it,
+// MorphologicOperations.cpp:3742-3750).
+//
+// The sequential algorithm pops the lowest non-empty of 256 FIFO queues; ties
+// are FIFO, so the result depends on the global pop order.  Two facts make an
+// exact parallel version possible:
+//
+//  1. Unknown pixels that are not black ("fg") split into DOMAINS — 4-connected
+//     components of unknown fg pixels.  Domains never touch each other, so the
+//     global pop sequence restricted to one domain equals that domain flooded
+//     on its own.  Only black unknown pixels ("U", the zeroed background of the
+//     masked colour image, whose label is 0 when it holds pixel 0) couple
+//     domains.
+//  2. Before the first U pixel is popped (time T_e) every domain is
+//     independent, and the global order of any two pops of different domains
+//     can be recovered from their own histories: a pop is "top-level" when its
+//     level is >= every earlier pop of its domain, otherwise it belongs to the
+//     dip of the last top-level pop; top-level pops are globally ordered by
+//     (level, push time) and push time is the pop time of the pusher, so
+//     comparing two pops walks their pushers' top-level origins (cmp_top).
+//
+// Phases (all on the device, no host round trip):
+//   P0  classify pixels, label domains (union-find), initial queue entries.
+//   P1  one thread floods each domain to completion; every push of a U pixel is
+//       kept as a "dummy" entry (it has no effect) so that its pop time is known.
+//   P2  the true entry of each U pixel is its earliest push; T_e is the
+//       earliest true U pop (a tournament with cmp_top); each domain's state at
+//       T_e is a prefix of its pop list (binary search with cmp_top).  At T_e
+//       the first U pixel e floods, at level 0, every black unknown pixel
+//       connected to it (region R) in FIFO BFS order; fg pixels that R touches
+//       are queued with R's label at their colour level, in that BFS order —
+//       a single-CTA, rank-ordered layer-synchronous BFS computes the exact
+//       order.  U pixels queued before T_e ("shells") and black regions R does
+//       not reach ("pockets") are attached to the domains they touch; domains
+//       that share a shell or a pocket are merged into one flood group.
+//   P3  one thread per group replays each member to its T_e state, merges the
+//       members' pending queues by push time, appends R's pushes and floods the
+//       group to completion.
+// Whenever an exactness condition fails (the first U pop at level 0, a
+// watershed-labelled first U pixel, an unowned active shell, an overflow) a
+// device flag makes the serial flood (ws_flood_serial) produce the result.
+#include <limits.h>
+
+#include "nsg_internal.cuh"
+
+namespace nsg {
+
+namespace {
+
+constexpr int WSHED = -1;
+constexpr int IN_QUEUE = -2;
+constexpr int kB = 256;
+
+// pixel flags
+constexpr uint8_t F_UNK = 1, F_U = 2, F_INIT = 4, F_FG = 8, F_BORDER = 16;
+// state bits at T_e
+constexpr uint8_t S_POPPED = 1, S_QUEUED = 2, S_R = 4, S_CERTAIN = 8, S_ACTIVE = 16, S_POCKET = 32;
+// rec_meta: level (8) | top << 8 | dir << 9
+__device__ __forceinline__ int m_level(int m) { return m & 255; }
+__device__ __forceinline__ int m_top(int m) { return (m >> 8) & 1; }
+__device__ __forceinline__ int m_dir(int m) { return (m >> 9) & 3; }
+
+// control block indices (ctrl + C_WS)
+enum {
+    W_FALLBACK = 0,
+    W_ND,
+    W_POOL,
+    W_E,
+    W_EP,
+    W_DOME,
+    W_LE,
+    W_X,
+    W_NCAND,
+    W_EVENT,
+    W_PEND,
+    W_LAYERS,
+};
+
+struct PW {
+    int H, W, n, pc;  // padded sizes, dummy-pool capacity
+    const int *mk;
+    const uint32_t *col;
+    int *outp;
+    int *ctl;  // ctrl + C_WS
+    int *status;
+    // per pixel
+    uint8_t *flags, *initlvl, *pside, *st, *fgimg;
+    int *domroot, *dom, *lab, *utrue, *inj, *claim, *uown, *proot, *fr0, *fr1, *popl, *isroot, *rank;
+    // per entry (n + pc)
+    int *next, *rparent, *rlocal, *rorigin, *rmeta;
+    // dummy pool
+    int *dpix, *ddom, *dseq, *dnextu;
+    // per domain
+    int *dsize, *doff, *bbx0, *bbx1, *bby0, *bby1, *npop, *cut, *sup, *mcount, *moff, *mfill, *mlist, *icount,
+        *ioff, *ifill, *ilist, *cand, *pend, *pend2;
+    unsigned long long *dfirst;
+};
+
+__device__ __forceinline__ int cdiff(uint32_t a, uint32_t b) {
+    int db = abs((int)(a & 255) - (int)(b & 255));
+    int dg = abs((int)((a >> 8) & 255) - (int)((b >> 8) & 255));
+    int dr = abs((int)((a >> 16) & 255) - (int)((b >> 16) & 255));
+    int d = db > dg ? db : dg;
+    return d > dr ? d : dr;
+}
+
+__device__ __forceinline__ void set_fallback(const PW &a, int code) { atomicCAS(a.ctl + W_FALLBACK, 0, code); }
+
+// ---------------------------------------------------------------- P0 --------
+__global__ void k_classify(PW a) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
+        int y = p / a.W, x = p - y * a.W;
+        uint8_t f = 0, il = 0;
+        if (y == 0 || y == a.H - 1 || x == 0 || x == a.W - 1) {
+            f = F_BORDER;
+        } else {
+            int m = a.mk[p];
+            if (m <= 0) {
+                f = F_UNK;
+                uint32_t c = a.col[p];
+                f |= c == 0 ? F_U : F_FG;
+                int idx = 256;
+                const int nb[4] = {p - 1, p + 1, p - a.W, p + a.W};
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    int q = nb[k];
+                    int qy = q / a.W, qx = q - qy * a.W;
+                    bool border = qy == 0 || qy == a.H - 1 || qx == 0 || qx == a.W - 1;
+                    if (!border && a.mk[q] > 0) {
+                        int t = cdiff(c, a.col[q]);
+                        idx = t < idx ? t : idx;
+                    }
+                }
+                if (idx < 256) {
+                    f |= F_INIT;
+                    il = (uint8_t)idx;
+                }
+            }
+        }
+        a.flags[p] = f;
+        a.initlvl[p] = il;
+        a.fgimg[p] = (f & F_FG) ? 1 : 0;
+        a.lab[p] = 0;
+        a.utrue[p] = -1;
+        a.pside[p] = 0;
+        a.st[p] = 0;
+        a.inj[p] = INT_MAX;
+        a.claim[p] = INT_MAX;
+        a.uown[p] = -1;
+        a.rlocal[p] = -1;
+        a.rparent[p] = -2;
+        a.isroot[p] = 0;
+        // per-domain arrays (indexed by domain id < n)
+        a.dsize[p] = 0;
+        a.bbx0[p] = INT_MAX;
+        a.bby0[p] = INT_MAX;
+        a.bbx1[p] = -1;
+        a.bby1[p] = -1;
+        a.dfirst[p] = ~0ull;
+        a.sup[p] = p;
+        a.mcount[p] = 0;
+        a.mfill[p] = 0;
+        a.icount[p] = 0;
+        a.ifill[p] = 0;
+        a.npop[p] = 0;
+        a.cut[p] = 0;
+    }
+}
+
+__global__ void k_roots(PW a) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x)
+        a.isroot[p] = (a.domroot[p] == p) ? 1 : 0;
+}
+
+__global__ void k_domains(PW a, const int *nd_total) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.ctl[W_ND] = *nd_total;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
+        int r = a.domroot[p];
+        int d = r >= 0 ? a.rank[r] : -1;
+        a.dom[p] = d;
+        if (d >= 0) {
+            int y = p / a.W, x = p - y * a.W;
+            atomicAdd(a.dsize + d, 1);
+            atomicMin(a.bbx0 + d, x);
+            atomicMax(a.bbx1 + d, x);
+            atomicMin(a.bby0 + d, y);
+            atomicMax(a.bby1 + d, y);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- queues ----
+struct Q {
+    int h[256], t[256];
+};
+__device__ __forceinline__ void q_init(Q &q) {
+    for (int i = 0; i < 256; ++i) q.h[i] = q.t[i] = -1;
+}
+__device__ __forceinline__ void q_push(Q &q, int *next, int lvl, int e) {
+    next[e] = -1;
+    if (q.t[lvl] < 0) q.h[lvl] = e;
+    else next[q.t[lvl]] = e;
+    q.t[lvl] = e;
+}
+
+// P1: flood domain d to completion, U pixels are dummies.
+__device__ void phase1_domain(const PW &a, int d);
+__global__ void __launch_bounds__(64) k_phase1(PW a) {
+    const int nd = a.ctl[W_ND];
+    for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < nd; d += gridDim.x * blockDim.x) phase1_domain(a, d);
+}
+
+__device__ void phase1_domain(const PW &a, int d) {
+    Q q;
+    q_init(q);
+    const int W = a.W, n = a.n;
+    for (int y = a.bby0[d]; y <= a.bby1[d]; ++y)
+        for (int x = a.bbx0[d]; x <= a.bbx1[d]; ++x) {
+            int p = y * W + x;
+            if (a.dom[p] != d || !(a.flags[p] & F_INIT)) continue;
+            int lv = a.initlvl[p];
+            a.rparent[p] = -1;
+            a.rmeta[p] = lv;
+            q_push(q, a.next, lv, p);
+            a.lab[p] = IN_QUEUE;
+        }
+    int active = 0, runmax = -1, lasttop = -1, local = 0, seq = 0;
+    const int base = a.doff[d];
+    for (;;) {
+        while (active < 256 && q.h[active] < 0) ++active;
+        if (active == 256) break;
+        int e = q.h[active];
+        q.h[active] = a.next[e];
+        if (q.h[active] < 0) q.t[active] = -1;
+        int meta = a.rmeta[e];
+        int lv = m_level(meta);
+        if (e >= n) {  // dummy U entry: position only
+            int k = e - n;
+            a.dseq[k] = seq++;
+            a.rlocal[e] = local;
+            int top = lv >= runmax;
+            a.rmeta[e] = meta | (top << 8);
+            a.rorigin[e] = top ? e : lasttop;
+            continue;
+        }
+        seq++;
+        const int p = e;
+        int top = lv >= runmax;
+        if (top) {
+            runmax = lv;
+            lasttop = p;
+        }
+        a.rmeta[p] = meta | (top << 8);
+        a.rorigin[p] = lasttop;
+        a.rlocal[p] = local;
+        a.popl[base + local] = p;
+        local++;
+        const int nb[4] = {p - 1, p + 1, p - W, p + W};
+        int lb = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            int qq = nb[k];
+            uint8_t fq = a.flags[qq];
+            int t = 0;
+            if (fq & F_BORDER) continue;
+            if (!(fq & F_UNK)) t = a.mk[qq];
+            else if (fq & F_FG) t = a.lab[qq];
+            if (t > 0) {
+                if (lb == 0) lb = t;
+                else if (t != lb) lb = WSHED;
+            }
+        }
+        a.lab[p] = lb;
+        if (lb <= 0) {
+            if (lb == 0) set_fallback(a, 9);
+            continue;
+        }
+        const uint32_t c = a.col[p];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            int qq = nb[k];
+            uint8_t fq = a.flags[qq];
+            if (!(fq & F_UNK)) continue;
+            if (fq & F_U) {
+                if (fq & F_INIT) continue;  // queued from the start
+                // already pushed by this domain from another side?
+                int side = k ^ 1;  // side of qq on which p lies (L<->R, U<->D)
+                int ps = (int)((__ldcg((const unsigned int *)(a.pside + (qq & ~3))) >> (8 * (qq & 3))) & 15u);
+                const int nq[4] = {qq - 1, qq + 1, qq - W, qq + W};
+                bool mine = false;
+                for (int s2 = 0; s2 < 4; ++s2)
+                    if ((ps >> s2) & 1)
+                        if (a.dom[nq[s2]] == d) mine = true;
+                if (mine) continue;
+                atomicOr((unsigned int *)(a.pside + (qq & ~3)), 1u << (8 * (qq & 3) + side));
+                int kk = atomicAdd(a.ctl + W_POOL, 1);
+                if (kk >= a.pc) {
+                    set_fallback(a, 4);
+                    continue;
+                }
+                int id = n + kk;
+                a.dpix[kk] = qq;
+                a.ddom[kk] = d;
+                a.rparent[id] = p;
+                a.rmeta[id] = cdiff(c, a.col[qq]) | (k << 9);
+                a.rlocal[id] = -1;
+                a.dnextu[kk] = atomicExch(a.utrue + qq, id);
+                int l2 = m_level(a.rmeta[id]);
+                q_push(q, a.next, l2, id);
+                if (l2 < active) active = l2;
+                continue;
+            }
+            if (a.lab[qq] != 0) continue;
+            int l2 = cdiff(c, a.col[qq]);
+            a.rparent[qq] = p;
+            a.rmeta[qq] = l2 | (k << 9);
+            q_push(q, a.next, l2, qq);
+            if (l2 < active) active = l2;
+            a.lab[qq] = IN_QUEUE;
+        }
+    }
+    a.npop[d] = local;
+}
+
+// ---------------------------------------------------------------- ordering --
+// x, y: top-level entries of different domains.  true if x pops first.
+__device__ bool cmp_top(const PW &a, int x, int y) {
+    for (int guard = 0; guard < (1 << 26); ++guard) {
+        int mx = a.rmeta[x], my = a.rmeta[y];
+        int lx = m_level(mx), ly = m_level(my);
+        if (lx != ly) return lx < ly;
+        int px = a.rparent[x], py = a.rparent[y];
+        if (px < 0 && py < 0) return x < y;  // initial entries: raster order
+        if (px < 0) return true;
+        if (py < 0) return false;
+        x = a.rorigin[px];
+        y = a.rorigin[py];
+    }
+    set_fallback(a, 10);
+    return false;
+}
+// push time of entry x before that of entry y (x, y of different domains or
+// of the same domain); parents are real pops
+__device__ bool push_before(const PW &a, int x, int dx, int y, int dy) {
+    int px = a.rparent[x], py = a.rparent[y];
+    if (px < 0 && py < 0) return x < y;  // both initial (raster); only real pixels are initial here
+    if (px < 0) return true;
+    if (py < 0) return false;
+    if (dx == dy) {
+        if (px == py) return m_dir(a.rmeta[x]) < m_dir(a.rmeta[y]);
+        return a.rlocal[px] < a.rlocal[py];
+    }
+    return cmp_top(a, a.rorigin[px], a.rorigin[py]);
+}
+
+// true entry of each U pixel: the earliest of its dummies
+__global__ void k_true_dummies(PW a) {
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < a.n; u += gridDim.x * blockDim.x) {
+        if (!(a.flags[u] & F_U)) continue;
+        if (a.flags[u] & F_INIT) {
+            // initial U entry: a top-level entry of its own
+            a.rparent[u] = -1;
+            a.rmeta[u] = a.initlvl[u] | (1 << 8);
+            a.rorigin[u] = u;
+            a.rlocal[u] = 0;
+            continue;
+        }
+        int best = a.utrue[u];
+        if (best < 0) continue;
+        for (int e = a.dnextu[best - a.n]; e >= 0; e = a.dnextu[e - a.n]) {
+            if (push_before(a, e, a.ddom[e - a.n], best, a.ddom[best - a.n])) best = e;
+        }
+        a.utrue[u] = best;
+        int k = best - a.n;
+        atomicMin(a.dfirst + a.ddom[k], ((unsigned long long)(unsigned)a.dseq[k] << 32) | (unsigned)best);
+    }
+}
+
+__global__ void k_candidates(PW a) {
+    const int nd = a.ctl[W_ND];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+        if (i < nd && a.dfirst[i] != ~0ull) {
+            int e = (int)(a.dfirst[i] & 0xffffffffu);
+            a.cand[atomicAdd(a.ctl + W_NCAND, 1)] = e;
+        }
+        if ((a.flags[i] & F_U) && (a.flags[i] & F_INIT)) a.cand[atomicAdd(a.ctl + W_NCAND, 1)] = i;
+    }
+}
+
+// single CTA: the earliest candidate pop
+__global__ void __launch_bounds__(1024) k_first_event(PW a) {
+    __shared__ int sh[1024];
+    const int nc = a.ctl[W_NCAND];
+    int best = -1;
+    for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+        int e = a.cand[i];
+        if (best < 0 || cmp_top(a, a.rorigin[e], a.rorigin[best])) best = e;
+    }
+    sh[threadIdx.x] = best;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            int x = sh[threadIdx.x], y = sh[threadIdx.x + s];
+            if (x < 0 || (y >= 0 && cmp_top(a, a.rorigin[y], a.rorigin[x]))) sh[threadIdx.x] = y;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        int e = sh[0];
+        a.ctl[W_E] = e;
+        a.ctl[W_EVENT] = e >= 0;
+        if (e >= 0) {
+            int ep = e >= a.n ? a.dpix[e - a.n] : e;
+            a.ctl[W_EP] = ep;
+            a.ctl[W_DOME] = e >= a.n ? a.ddom[e - a.n] : -1;
+            a.ctl[W_LE] = m_level(a.rmeta[e]);
+            if (m_level(a.rmeta[e]) < 1) set_fallback(a, 1);
+        }
+    }
+}
+
+__global__ void k_cuts(PW a) {
+    const int nd = a.ctl[W_ND];
+    if (!a.ctl[W_EVENT] || a.ctl[W_FALLBACK]) return;
+    const int e = a.ctl[W_E];
+    const int oe = a.rorigin[e];
+    for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < nd; d += gridDim.x * blockDim.x) {
+        if (d == a.ctl[W_DOME]) {
+            a.cut[d] = a.rlocal[e];
+            continue;
+        }
+        int lo = 0, hi = a.npop[d];  // first index whose pop is not before e
+        const int base = a.doff[d];
+        while (lo < hi) {
+            int mid = (lo + hi) >> 1;
+            int p = a.popl[base + mid];
+            if (cmp_top(a, a.rorigin[p], oe)) lo = mid + 1;
+            else hi = mid;
+        }
+        a.cut[d] = lo;
+    }
+}
+
+// state of every pixel at T_e
+__global__ void k_state(PW a) {
+    if (!a.ctl[W_EVENT] || a.ctl[W_FALLBACK]) return;
+    const int ep = a.ctl[W_EP];
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
+        uint8_t f = a.flags[p];
+        uint8_t s = 0;
+        if (f & F_FG) {
+            int d = a.dom[p];
+            int lc = a.rlocal[p];
+            bool popped = lc >= 0 && lc < a.cut[d];
+            if (popped) s |= S_POPPED;
+            else {
+                int par = a.rparent[p];
+                bool pushed = par == -1 || (par >= 0 && a.rlocal[par] >= 0 && a.rlocal[par] < a.cut[d]);
+                if (pushed) s |= S_QUEUED;
+            }
+        } else if (f & F_U) {
+            if (p == ep) {
+                s |= S_R;
+            } else if (f & F_INIT) {
+                s |= S_QUEUED;
+            } else {
+                int e = a.utrue[p];
+                if (e >= 0) {
+                    int par = a.rparent[e];
+                    int dd = a.ddom[e - a.n];
+                    if (a.rlocal[par] < a.cut[dd]) s |= S_QUEUED;
+                }
+            }
+        }
+        a.st[p] = s;
+    }
+}
+
+__global__ void k_event_label(PW a) {
+    if (threadIdx.x || blockIdx.x) return;
+    if (!a.ctl[W_EVENT] || a.ctl[W_FALLBACK]) return;
+    const int ep = a.ctl[W_EP];
+    const int W = a.W;
+    const int nb[4] = {ep - 1, ep + 1, ep - W, ep + W};
+    int lb = 0;
+    for (int k = 0; k < 4; ++k) {
+        int q = nb[k];
+        uint8_t f = a.flags[q];
+        int t = 0;
+        if (f & F_BORDER) continue;
+        if (!(f & F_UNK)) t = a.mk[q];
+        else if ((f & F_FG) && (a.st[q] & S_POPPED)) t = a.lab[q];
+        if (t > 0) {
+            if (lb == 0) lb = t;
+            else if (t != lb) lb = WSHED;
+        }
+    }
+    a.ctl[W_X] = lb;
+    if (lb <= 0) set_fallback(a, 2);
+}
+
+// ------------------------------------------------------ rank-ordered BFS ----
+__device__ int cta_exclusive_scan(int v, int *sh, int &total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) sh[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0;
+        int z = w;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, z, d);
+            if (lane >= d) z += y;
+        }
+        sh[lane] = z - w;
+        if (lane == 31) sh[32] = z;
+    }
+    __syncthreads();
+    int r = sh[warp] + x - v;
+    total = sh[32];
+    __syncthreads();
+    return r;
+}
+
+// FIFO BFS from e over black unknown pixels that are not queued at T_e: the
+// pop rank of each R pixel is its position in the frontier sequence; every
+// state-0 fg neighbour records the smallest (rank * 4 + direction) that
+// touches it, which is the order in which R pushes it.
+__global__ void __launch_bounds__(1024) k_bfs(PW a) {
+    __shared__ int sh[40];
+    if (!a.ctl[W_EVENT] || a.ctl[W_FALLBACK]) return;
+    const int W = a.W;
+    int *F0 = a.fr0, *F1 = a.fr1;
+    int s = 1, base = 0, layers = 0;
+    if (threadIdx.x == 0) F0[0] = a.ctl[W_EP];
+    __syncthreads();
+    const int off[4] = {-1, 1, -W, W};
+    while (s > 0) {
+        const int per = (s + blockDim.x - 1) / blockDim.x;
+        const int i0 = threadIdx.x * per, i1 = min(s, i0 + per);
+        for (int i = i0; i < i1; ++i) {
+            int r = __ldcg(F0 + i);
+            for (int k = 0; k < 4; ++k) {
+                int qq = r + off[k];
+                uint8_t f = a.flags[qq];
+                if (!(f & F_UNK)) continue;
+                uint8_t sq = __ldcg(a.st + qq);
+                if (f & F_U) {
+                    if (sq & (S_QUEUED | S_R)) continue;
+                    atomicMin(a.claim + qq, i * 4 + k);
+                } else if (!(sq & (S_POPPED | S_QUEUED))) {
+                    atomicMin(a.inj + qq, (base + i) * 4 + k);
+                }
+            }
+        }
+        __syncthreads();
+        int cnt = 0;
+        for (int i = i0; i < i1; ++i) {
+            int r = __ldcg(F0 + i);
+            for (int k = 0; k < 4; ++k) {
+                int qq = r + off[k];
+                if ((a.flags[qq] & F_U) && __ldcg(a.claim + qq) == i * 4 + k) ++cnt;
+            }
+        }
+        int total;
+        int pos = cta_exclusive_scan(cnt, sh, total);
+        for (int i = i0; i < i1; ++i) {
+            int r = __ldcg(F0 + i);
+            for (int k = 0; k < 4; ++k) {
+                int qq = r + off[k];
+                if ((a.flags[qq] & F_U) && __ldcg(a.claim + qq) == i * 4 + k) {
+                    F1[pos++] = qq;
+                    a.st[qq] |= S_R;
+                    a.claim[qq] = INT_MAX;
+                }
+            }
+        }
+        __threadfence_block();
+        __syncthreads();
+        int *t = F0;
+        F0 = F1;
+        F1 = t;
+        base += s;
+        s = total;
+        ++layers;
+    }
+    if (threadIdx.x == 0) a.ctl[W_LAYERS] = layers;
+}
+
+// shells: U pixels queued at T_e
+__global__ void k_shells(PW a) {
+    if (!a.ctl[W_EVENT] || a.ctl[W_FALLBACK]) return;
+    const int X = a.ctl[W_X];
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < a.n; u += gridDim.x * blockDim.x) {
+        if (!(a.flags[u] & F_U)) continue;
+        uint8_t s = a.st[u];
+        if (!(s & S_QUEUED)) continue;
+        const int nb[4] = {u - 1, u + 1, u - a.W, u + a.W};
+        bool adjR = false;
+        int mk1 = 0;
+        bool two = false;
+        for (int k = 0; k < 4; ++k) {
+            int q = nb[k];
+            if (a.st[q] & S_R) adjR = true;
+            uint8_t f = a.flags[q];
+            if (!(f & (F_UNK | F_BORDER))) {
+                int m = a.mk[q];
+                if (mk1 == 0) mk1 = m;
+                else if (m != mk1) two = true;
+            }
+        }
+        int Y;
+        int owner = -1;
+        if (a.flags[u] & F_INIT) {
+            Y = mk1;
+        } else {
+            int e = a.utrue[u];
+            Y = a.lab[a.rparent[e]];
+            owner = a.ddom[e - a.n];
+        }
+        if ((adjR && Y > 0 && Y != X) || two) {
+            a.st[u] = s | S_CERTAIN;
+            continue;
+        }
+        if (owner < 0) {
+            set_fallback(a, 3);
+            continue;
+        }
+        a.st[u] = s | S_ACTIVE;
+        a.uown[u] = owner;
+    }
+}
+
+__global__ void k_pocket_img(PW a, uint8_t *img) {
+    const bool on = a.ctl[W_EVENT] && !a.ctl[W_FALLBACK];
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
+        bool pk = on && (a.flags[p] & F_U) && !(a.st[p] & (S_QUEUED | S_R));
+        img[p] = pk ? 1 : 0;
+        if (pk) a.st[p] |= S_POCKET;
+    }
+}
+
+__device__ __forceinline__ int sfind(int *par, int x) {
+    for (;;) {
+        int p = __ldcg(par + x);
+        if (p == x) return x;
+        x = p;
+    }
+}
+__device__ void sunite(int *par, int a_, int b_) {
+    for (int guard = 0; guard < (1 << 24); ++guard) {
+        a_ = sfind(par, a_);
+        b_ = sfind(par, b_);
+        if (a_ == b_) return;
+        if (a_ < b_) {
+            int t = a_;
+            a_ = b_;
+            b_ = t;
+        }
+        int old = atomicMin(par + a_, b_);
+        if (old == a_) return;
+        a_ = old;
+    }
+}
+
+// pocket owners: first domain (or active-shell owner) touching the pocket;
+// every other one is merged with it
+__global__ void k_pocket_owner(PW a, int *powner) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
+        if (!(a.st[p] & S_POCKET)) continue;
+        int r = a.proot[p];
+        const int nb[4] = {p - 1, p + 1, p - a.W, p + a.W};
+        for (int k = 0; k < 4; ++k) {
+            int q = nb[k];
+            int d = -1;
+            if (a.flags[q] & F_FG) d = a.dom[q];
+            else if (a.st[q] & S_ACTIVE) d = a.uown[q];
+            else if (a.st[q] & S_R) set_fallback(a, 7);
+            if (d < 0) continue;
+            int old = atomicCAS(powner + r, -1, d);
+            if (old != -1 && old != d) sunite(a.sup, old, d);
+        }
+    }
+}
+__global__ void k_shell_unions(PW a, const int *powner) {
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < a.n; u += gridDim.x * blockDim.x) {
+        if (a.st[u] & S_POCKET) {
+            int o = powner[a.proot[u]];
+            a.uown[u] = o;  // -1: never entered
+            continue;
+        }
+        if (!(a.st[u] & S_ACTIVE)) continue;
+        int o = a.uown[u];
+        const int nb[4] = {u - 1, u + 1, u - a.W, u + a.W};
+        for (int k = 0; k < 4; ++k) {
+            int q = nb[k];
+            if (a.flags[q] & F_FG) sunite(a.sup, o, a.dom[q]);
+            else if (a.st[q] & S_ACTIVE) sunite(a.sup, o, a.uown[q]);
+            else if ((a.st[q] & S_POCKET) && powner[a.proot[q]] >= 0) sunite(a.sup, o, powner[a.proot[q]]);
+        }
+    }
+}
+
+__global__ void k_sup_flatten(PW a) {
+    const int nd = a.ctl[W_ND];
+    for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < nd; d += gridDim.x * blockDim.x)
+        a.sup[d] = sfind(a.sup, d);
+}
+__global__ void k_groups(PW a) {
+    const int nd = a.ctl[W_ND];
+    for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < nd; d += gridDim.x * blockDim.x) {
+        int r = sfind(a.sup, d);
+        atomicAdd(a.mcount + r, 1);
+    }
+}
+__global__ void k_groups2(PW a) {
+    const int nd = a.ctl[W_ND];
+    for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < nd; d += gridDim.x * blockDim.x) {
+        int r = sfind(a.sup, d);
+        a.mlist[a.moff[r] + atomicAdd(a.mfill + r, 1)] = d;
+    }
+}
+__global__ void k_inj_count(PW a, int pass) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
+        if (a.inj[p] == INT_MAX) continue;
+        int r = a.sup[a.dom[p]];
+        if (pass == 0) atomicAdd(a.icount + r, 1);
+        else a.ilist[a.ioff[r] + atomicAdd(a.ifill + r, 1)] = p;
+    }
+}
+__global__ void k_reset_owned_u(PW a) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x)
+        if ((a.st[p] & (S_ACTIVE | S_POCKET)) && a.uown[p] >= 0) a.lab[p] = 0;
+}
+
+// ---------------------------------------------------------------- P3 --------
+__device__ __forceinline__ bool owned(const PW &a, int q, int S) {
+    uint8_t f = a.flags[q];
+    if (f & F_FG) return a.sup[a.dom[q]] == S;
+    if (f & F_U) {
+        int o = a.uown[q];
+        return o >= 0 && (a.st[q] & (S_ACTIVE | S_POCKET)) && a.sup[o] == S;
+    }
+    return false;
+}
+
+// replay domain d up to its T_e state (pre-T_e rules)
+__device__ bool replay(const PW &a, int d, Q &q, int &active) {
+    const int W = a.W;
+    for (int y = a.bby0[d]; y <= a.bby1[d]; ++y)
+        for (int x = a.bbx0[d]; x <= a.bbx1[d]; ++x) {
+            int p = y * W + x;
+            if (a.dom[p] == d) a.lab[p] = 0;
+        }
+    for (int y = a.bby0[d]; y <= a.bby1[d]; ++y)
+        for (int x = a.bbx0[d]; x <= a.bbx1[d]; ++x) {
+            int p = y * W + x;
+            if (a.dom[p] != d || !(a.flags[p] & F_INIT)) continue;
+            q_push(q, a.next, a.initlvl[p], p);
+            a.lab[p] = IN_QUEUE;
+        }
+    active = 0;
+    const int cutd = a.cut[d];
+    for (int local = 0; local < cutd;) {
+        while (active < 256 && q.h[active] < 0) ++active;
+        if (active == 256) return false;
+        int e = q.h[active];
+        q.h[active] = a.next[e];
+        if (q.h[active] < 0) q.t[active] = -1;
+        const int p = e;
+        if (!(a.flags[p] & F_FG)) return false;  // no U pop before T_e
+        ++local;
+        const int nb[4] = {p - 1, p + 1, p - W, p + W};
+        int lb = 0;
+        for (int k = 0; k < 4; ++k) {
+            int qq = nb[k];
+            uint8_t fq = a.flags[qq];
+            int t = 0;
+            if (fq & F_BORDER) continue;
+            if (!(fq & F_UNK)) t = a.mk[qq];
+            else if (fq & F_FG) t = a.lab[qq];
+            if (t > 0) {
+                if (lb == 0) lb = t;
+                else if (t != lb) lb = WSHED;
+            }
+        }
+        a.lab[p] = lb;
+        if (lb == 0) return false;
+        if (lb == WSHED) continue;
+        const uint32_t c = a.col[p];
+        for (int k = 0; k < 4; ++k) {
+            int qq = nb[k];
+            uint8_t fq = a.flags[qq];
+            if (!(fq & F_UNK)) continue;
+            if (fq & F_U) {
+                if (!(a.st[qq] & S_ACTIVE)) continue;
+                int te = a.utrue[qq];
+                if (te < a.n || a.ddom[te - a.n] != d) continue;
+                if (a.lab[qq] != 0) continue;
+                int l2 = cdiff(c, a.col[qq]);
+                a.rparent[qq] = p;
+                a.rmeta[qq] = l2 | (k << 9);
+                q_push(q, a.next, l2, qq);
+                if (l2 < active) active = l2;
+                a.lab[qq] = IN_QUEUE;
+                continue;
+            }
+            if (a.lab[qq] != 0) continue;
+            int l2 = cdiff(c, a.col[qq]);
+            q_push(q, a.next, l2, qq);
+            if (l2 < active) active = l2;
+            a.lab[qq] = IN_QUEUE;
+        }
+    }
+    return true;
+}
+
+__device__ void phase3_group(const PW &a, int S);
+__global__ void __launch_bounds__(64) k_phase3(PW a) {
+    const int nd = a.ctl[W_ND];
+    if (a.ctl[W_FALLBACK] || !a.ctl[W_EVENT]) return;
+    for (int S = blockIdx.x * blockDim.x + threadIdx.x; S < nd; S += gridDim.x * blockDim.x)
+        if (a.mcount[S] > 0) phase3_group(a, S);
+}
+__device__ void phase3_group(const PW &a, int S) {
+    const int nm = a.mcount[S];
+    const int *mem = a.mlist + a.moff[S];
+    const int X = a.ctl[W_X];
+    const int W = a.W;
+    Q q;
+    q_init(q);
+    int active = 0;
+    if (nm == 1) {
+        if (!replay(a, mem[0], q, active)) {
+            set_fallback(a, 11);
+            return;
+        }
+    } else {
+        // replay every member, collect pending entries, merge them by push time
+        int total = 0;
+        for (int m = 0; m < nm; ++m) total += a.dsize[mem[m]] + 4 * a.dsize[mem[m]];
+        int pb = atomicAdd(a.ctl + W_PEND, total);
+        if (pb + total > a.n) {
+            set_fallback(a, 6);
+            return;
+        }
+        int *pend = a.pend + pb, *tmp = a.pend2 + pb;
+        int np = 0;
+        for (int m = 0; m < nm; ++m) {
+            Q qm;
+            q_init(qm);
+            int act = 0;
+            if (!replay(a, mem[m], qm, act)) {
+                set_fallback(a, 11);
+                return;
+            }
+            for (int lv = 0; lv < 256; ++lv)
+                for (int e = qm.h[lv]; e >= 0; e = a.next[e]) pend[np++] = e;
+        }
+        // bottom-up merge sort by (level, push time)
+        for (int w = 1; w < np; w <<= 1) {
+            for (int lo = 0; lo < np; lo += 2 * w) {
+                int mid = min(lo + w, np), hi = min(lo + 2 * w, np);
+                int i = lo, j = mid, k = lo;
+                while (i < mid && j < hi) {
+                    int x = pend[i], y = pend[j];
+                    int lx = m_level(a.rmeta[x]), ly = m_level(a.rmeta[y]);
+                    int dx = (a.flags[x] & F_FG) ? a.dom[x] : a.ddom[a.utrue[x] - a.n];
+                    int dy = (a.flags[y] & F_FG) ? a.dom[y] : a.ddom[a.utrue[y] - a.n];
+                    bool yfirst = ly < lx || (ly == lx && push_before(a, y, dy, x, dx));
+                    tmp[k++] = yfirst ? pend[j++] : pend[i++];
+                }
+                while (i < mid) tmp[k++] = pend[i++];
+                while (j < hi) tmp[k++] = pend[j++];
+                for (int t = lo; t < hi; ++t) pend[t] = tmp[t];
+            }
+        }
+        for (int i = 0; i < np; ++i) {
+            int e = pend[i];
+            q_push(q, a.next, m_level(a.rmeta[e]), e);
+        }
+        active = 0;
+    }
+    // T_e: R's pushes into this group, in BFS order
+    {
+        const int ni = a.icount[S];
+        int *il = a.ilist + a.ioff[S];
+        for (int i = 1; i < ni; ++i) {  // insertion sort by BFS key
+            int v = il[i], kv = a.inj[v], j = i - 1;
+            while (j >= 0 && a.inj[il[j]] > kv) {
+                il[j + 1] = il[j];
+                --j;
+            }
+            il[j + 1] = v;
+        }
+        for (int i = 0; i < ni; ++i) {
+            int p = il[i];
+            if (a.lab[p] != 0) {
+                set_fallback(a, 12);
+                return;
+            }
+            int l2 = cdiff(a.col[p], 0u);
+            q_push(q, a.next, l2, p);
+            a.lab[p] = IN_QUEUE;
+            if (l2 < active) active = l2;
+        }
+    }
+    // flood after T_e
+    for (long long guard = 0;; ++guard) {
+        while (active < 256 && q.h[active] < 0) ++active;
+        if (active == 256) break;
+        int e = q.h[active];
+        q.h[active] = a.next[e];
+        if (q.h[active] < 0) q.t[active] = -1;
+        const int p = e;
+        const int nb[4] = {p - 1, p + 1, p - W, p + W};
+        int lb = 0;
+        for (int k = 0; k < 4; ++k) {
+            int qq = nb[k];
+            uint8_t fq = a.flags[qq];
+            int t = 0;
+            if (fq & F_BORDER) continue;
+            if (!(fq & F_UNK)) t = a.mk[qq];
+            else if (a.st[qq] & S_R) t = X;
+            else if (owned(a, qq, S)) t = a.lab[qq];
+            if (t > 0) {
+                if (lb == 0) lb = t;
+                else if (t != lb) lb = WSHED;
+            }
+        }
+        a.lab[p] = lb;
+        if (lb == 0) {
+            set_fallback(a, 13);
+            return;
+        }
+        if (lb == WSHED) continue;
+        const uint32_t c = a.col[p];
+        for (int k = 0; k < 4; ++k) {
+            int qq = nb[k];
+            uint8_t fq = a.flags[qq];
+            if (!(fq & F_UNK)) continue;
+            uint8_t sq = a.st[qq];
+            if (sq & (S_R | S_CERTAIN)) continue;
+            if (!owned(a, qq, S)) {
+                set_fallback(a, 5);
+                return;
+            }
+            if (a.lab[qq] != 0) continue;
+            int l2 = cdiff(c, a.col[qq]);
+            q_push(q, a.next, l2, qq);
+            if (l2 < active) active = l2;
+            a.lab[qq] = IN_QUEUE;
+        }
+    }
+}
+
+// final padded labels
+__global__ void k_assemble(PW a) {
+    const int event = a.ctl[W_EVENT];
+    const int X = a.ctl[W_X];
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
+        uint8_t f = a.flags[p];
+        int v;
+        if (f & F_BORDER) v = WSHED;
+        else if (!(f & F_UNK)) v = a.mk[p];
+        else if (f & F_FG) v = a.lab[p];
+        else if (!event) v = 0;
+        else {
+            uint8_t s = a.st[p];
+            if (s & S_R) v = X;
+            else if (s & S_CERTAIN) v = WSHED;
+            else if ((s & (S_ACTIVE | S_POCKET)) && a.uown[p] >= 0) v = a.lab[p];
+            else v = 0;
+        }
+        a.outp[p] = v == IN_QUEUE ? 0 : v;
+    }
+}
+
+// ------------------------------------------------------------- fallback -----
+__global__ void k_copy_if(const int *mk, int *outp, int n, const int *flag) {
+    if (*flag == 0) return;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) outp[p] = mk[p];
+}
+
+__global__ void k_serial(int *m, const uint32_t *col, int *next, int H, int W, long long budget, int *status,
+                         const int *flag) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (flag && *flag == 0) return;
+    int qh[256], qt[256];
+    for (int i = 0; i < 256; ++i) qh[i] = qt[i] = -1;
+    auto push = [&](int idx, int ofs) {
+        next[ofs] = -1;
+        if (qt[idx] < 0) qh[idx] = ofs;
+        else next[qt[idx]] = ofs;
+        qt[idx] = ofs;
+    };
+    for (int j = 0; j < W; ++j) m[j] = m[j + (int64_t)W * (H - 1)] = WSHED;
+    for (int i = 1; i < H - 1; ++i) {
+        int *row = m + (int64_t)i * W;
+        row[0] = row[W - 1] = WSHED;
+        for (int j = 1; j < W - 1; ++j) {
+            int *p = row + j;
+            if (p[0] < 0) p[0] = 0;
+            if (p[0] == 0 && (p[-1] > 0 || p[1] > 0 || p[-W] > 0 || p[W] > 0)) {
+                int ofs = i * W + j;
+                uint32_t c = col[ofs];
+                int idx = 256, t;
+                if (p[-1] > 0) idx = cdiff(c, col[ofs - 1]);
+                if (p[1] > 0) {
+                    t = cdiff(c, col[ofs + 1]);
+                    idx = idx < t ? idx : t;
+                }
+                if (p[-W] > 0) {
+                    t = cdiff(c, col[ofs - W]);
+                    idx = idx < t ? idx : t;
+                }
+                if (p[W] > 0) {
+                    t = cdiff(c, col[ofs + W]);
+                    idx = idx < t ? idx : t;
+                }
+                push(idx, ofs);
+                p[0] = IN_QUEUE;
+            }
+        }
+    }
+    int active = 0;
+    while (active < 256 && qh[active] < 0) ++active;
+    if (active == 256) return;
+    long long steps = 0;
+    for (;;) {
+        if (qh[active] < 0) {
+            int i;
+            for (i = active + 1; i < 256; ++i)
+                if (qh[i] >= 0) break;
+            if (i == 256) break;
+            active = i;
+        }
+        if (++steps > budget) {
+            atomicOr(status, DEV_TIMEOUT);
+            return;
+        }
+        int ofs = qh[active];
+        qh[active] = next[ofs];
+        if (qh[active] < 0) qt[active] = -1;
+        int *p = m + ofs;
+        int lab = 0, t;
+        t = p[-1];
+        if (t > 0) lab = t;
+        t = p[1];
+        if (t > 0) {
+            if (lab == 0) lab = t;
+            else if (t != lab) lab = WSHED;
+        }
+        t = p[-W];
+        if (t > 0) {
+            if (lab == 0) lab = t;
+            else if (t != lab) lab = WSHED;
+        }
+        t = p[W];
+        if (t > 0) {
+            if (lab == 0) lab = t;
+            else if (t != lab) lab = WSHED;
+        }
+        p[0] = lab;
+        if (lab == WSHED) continue;
+        uint32_t c = col[ofs];
+        if (p[-1] == 0) {
+            t = cdiff(c, col[ofs - 1]);
+            push(t, ofs - 1);
+            active = active < t ? active : t;
+            p[-1] = IN_QUEUE;
+        }
+        if (p[1] == 0) {
+            t = cdiff(c, col[ofs + 1]);
+            push(t, ofs + 1);
+            active = active < t ? active : t;
+            p[1] = IN_QUEUE;
+        }
+        if (p[-W] == 0) {
+            t = cdiff(c, col[ofs - W]);
+            push(t, ofs - W);
+            active = active < t ? active : t;
+            p[-W] = IN_QUEUE;
+        }
+        if (p[W] == 0) {
+            t = cdiff(c, col[ofs + W]);
+            push(t, ofs + W);
+            active = active < t ? active : t;
+            p[W] = IN_QUEUE;
+        }
+    }
+}
+
+int blocks(Ctx &c, int64_t n) {
+    int64_t g = (n + kB - 1) / kB;
+    int64_t cap = (int64_t)c.sm_count * 16;
+    return (int)(g < 1 ? 1 : (g < cap ? g : cap));
+}
+
+struct Carve {
+    char *p;
+    size_t used = 0;
+    template <typename T>
+    T *take(size_t count) {
+        size_t b = (count * sizeof(T) + 255) & ~(size_t)255;
+        T *r = reinterpret_cast<T *>(p + used);
+        used += b;
+        return r;
+    }
+};
+
+void carve(PW &a, char *base, size_t *used_out) {
+    const size_t n = (size_t)a.n, np = (size_t)a.n + a.pc, pc = (size_t)a.pc;
+    Carve cv{base};
+    a.flags = cv.take<uint8_t>(n);
+    a.initlvl = cv.take<uint8_t>(n);
+    a.pside = cv.take<uint8_t>(n + 4);
+    a.st = cv.take<uint8_t>(n);
+    a.fgimg = cv.take<uint8_t>(n);
+    a.domroot = cv.take<int>(n);
+    a.dom = cv.take<int>(n);
+    a.lab = cv.take<int>(n);
+    a.utrue = cv.take<int>(n);
+    a.inj = cv.take<int>(n);
+    a.claim = cv.take<int>(n);
+    a.uown = cv.take<int>(n);
+    a.proot = cv.take<int>(n);
+    a.fr0 = cv.take<int>(n);
+    a.fr1 = cv.take<int>(n);
+    a.popl = cv.take<int>(n);
+    a.isroot = cv.take<int>(n);
+    a.rank = cv.take<int>(n);
+    a.next = cv.take<int>(np);
+    a.rparent = cv.take<int>(np);
+    a.rlocal = cv.take<int>(np);
+    a.rorigin = cv.take<int>(np);
+    a.rmeta = cv.take<int>(np);
+    a.dpix = cv.take<int>(pc);
+    a.ddom = cv.take<int>(pc);
+    a.dseq = cv.take<int>(pc);
+    a.dnextu = cv.take<int>(pc);
+    a.dsize = cv.take<int>(n);
+    a.doff = cv.take<int>(n);
+    a.bbx0 = cv.take<int>(n);
+    a.bbx1 = cv.take<int>(n);
+    a.bby0 = cv.take<int>(n);
+    a.bby1 = cv.take<int>(n);
+    a.npop = cv.take<int>(n);
+    a.cut = cv.take<int>(n);
+    a.sup = cv.take<int>(n);
+    a.mcount = cv.take<int>(n);
+    a.moff = cv.take<int>(n);
+    a.mfill = cv.take<int>(n);
+    a.mlist = cv.take<int>(n);
+    a.icount = cv.take<int>(n);
+    a.ioff = cv.take<int>(n);
+    a.ifill = cv.take<int>(n);
+    a.ilist = cv.take<int>(n);
+    a.cand = cv.take<int>(n);
+    a.pend = cv.take<int>(n);
+    a.pend2 = cv.take<int>(n);
+    a.dfirst = cv.take<unsigned long long>(n);
+    *used_out = cv.used;
+}
+
+}  // namespace
+
+size_t pws_workspace_bytes(int64_t npad) {
+    PW a;
+    a.n = (int)npad;
+    a.pc = (int)(npad / 2 + 4096);
+    size_t used = 0;
+    carve(a, nullptr, &used);
+    return used + 4096;
+}
+
+int ws_flood_serial_launch(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int W, bool conditional,
+                           cudaStream_t s) {
+    const int n = H * W;
+    int *flag = conditional ? c.ws.ctrl + C_WS + W_FALLBACK : nullptr;
+    // the flood's links reuse the start of the workspace: nothing there is read
+    // once the serial flood runs
+    int *next = (int *)c.ws.wsb;
+    if (conditional) {
+        k_copy_if<<<blocks(c, n), kB, 0, s>>>(mk, outp, n, flag);
+    } else {
+        cudaMemcpyAsync(outp, mk, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+    }
+    k_serial<<<1, 32, 0, s>>>(outp, col, next, H, W, c.spin_budget * 64, c.ws.ctrl + C_STATUS, flag);
+    NSG_LAUNCH_CHECK(c);
+    return NSG_SUCCESS;
+}
+
+int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int W, cudaStream_t s) {
+    PW a;
+    a.H = H;
+    a.W = W;
+    a.n = H * W;
+    a.pc = a.n / 2 + 4096;
+    a.mk = mk;
+    a.col = col;
+    a.outp = outp;
+    a.ctl = c.ws.ctrl + C_WS;
+    a.status = c.ws.ctrl + C_STATUS;
+    size_t used = 0;
+    carve(a, c.ws.wsb, &used);
+    if (used > c.ws.wsb_bytes) {
+        c.last_error = "watershed workspace too small";
+        return NSG_ERR_OOM;
+    }
+    const int n = a.n;
+    const int g = blocks(c, n);
+    NSG_CUDA_TRY(c, cudaMemsetAsync(a.ctl, 0, 64 * sizeof(int), s));
+    k_classify<<<g, kB, 0, s>>>(a);
+    NSG_LAUNCH_CHECK(c);
+    NSG_TRY(ccl_u8(c, a.fgimg, a.domroot, H, W, 4, CCL_NONZERO, s));
+    k_roots<<<g, kB, 0, s>>>(a);
+    NSG_TRY(exclusive_scan_i32(c, a.isroot, a.rank, n, a.ctl + W_ND, s));
+    k_domains<<<g, kB, 0, s>>>(a, a.ctl + W_ND);
+    NSG_TRY(exclusive_scan_i32(c, a.dsize, a.doff, n, nullptr, s));
+    NSG_LAUNCH_CHECK(c);
+    // P1: one thread per domain (the grid covers the largest possible count)
+    const int gd = c.sm_count * 32;  // per-domain kernels: grid-stride over the domain count
+    k_phase1<<<gd, 64, 0, s>>>(a);
+    NSG_LAUNCH_CHECK(c);
+    // P2
+    k_true_dummies<<<g, kB, 0, s>>>(a);
+    k_candidates<<<g, kB, 0, s>>>(a);
+    k_first_event<<<1, 1024, 0, s>>>(a);
+    k_cuts<<<gd / 4, 256, 0, s>>>(a);
+    NSG_LAUNCH_CHECK(c);
+    k_state<<<g, kB, 0, s>>>(a);
+    k_event_label<<<1, 32, 0, s>>>(a);
+    k_bfs<<<1, 1024, 0, s>>>(a);
+    NSG_LAUNCH_CHECK(c);
+    k_shells<<<g, kB, 0, s>>>(a);
+    uint8_t *pimg = a.fgimg;  // reuse: the domain image is no longer needed
+    k_pocket_img<<<g, kB, 0, s>>>(a, pimg);
+    NSG_TRY(ccl_u8(c, pimg, a.proot, H, W, 4, CCL_NONZERO, s));
+    int *powner = a.claim;  // BFS claims are no longer needed
+    NSG_CUDA_TRY(c, cudaMemsetAsync(powner, 0xff, sizeof(int) * (size_t)n, s));
+    k_pocket_owner<<<g, kB, 0, s>>>(a, powner);
+    k_shell_unions<<<g, kB, 0, s>>>(a, powner);
+    k_sup_flatten<<<g, kB, 0, s>>>(a);
+    k_groups<<<g, kB, 0, s>>>(a);
+    NSG_TRY(exclusive_scan_i32(c, a.mcount, a.moff, n, nullptr, s));
+    k_groups2<<<g, kB, 0, s>>>(a);
+    k_inj_count<<<g, kB, 0, s>>>(a, 0);
+    NSG_TRY(exclusive_scan_i32(c, a.icount, a.ioff, n, nullptr, s));
+    k_inj_count<<<g, kB, 0, s>>>(a, 1);
+    k_reset_owned_u<<<g, kB, 0, s>>>(a);
+    NSG_LAUNCH_CHECK(c);
+    k_phase3<<<gd, 64, 0, s>>>(a);
+    k_assemble<<<g, kB, 0, s>>>(a);
+    NSG_LAUNCH_CHECK(c);
+    // exact serial flood when a fast-path condition failed
+    return ws_flood_serial_launch(c, mk, col, outp, H, W, true, s);
+}
+
+}  // namespace nsg

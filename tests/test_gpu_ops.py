@@ -207,3 +207,80 @@ def test_watershed2(cuda, orc, shape, conn):
     bgr = synth.colorize_mask(m, seed=0x5EED0000)
     got = N(MO.watershed2(T(bgr), T(d2), conn))
     np.testing.assert_array_equal(got, orc.watershed2(bgr, d2, conn))
+
+
+def _ws_diag():
+    import ctypes as C
+    from nscale_gb300.context import get_context, stream_handle
+    ctx = get_context(1, 1)
+    out = (C.c_int * 16)()
+    ctx.check(ctx.L.nsg_watershed_diagnostics(ctx.h, out, stream_handle()))
+    return list(out)
+
+
+def _pipeline_ws_inputs(orc, rows, cols, seed):
+    from nscale_gb300 import synth
+    img = synth.he_tile(rows, cols, seed)
+    _, _, _, _, d = orc.segment_nuclei(img, dump_stages=("seg_big", "distance2"))
+    nuclei = img.copy()
+    nuclei[d["seg_big"] == 0] = 0
+    return nuclei, d["distance2"]
+
+
+@pytest.mark.parametrize("shape,seed", [((512, 512), 0x5EED0000), ((1024, 1024), 0x5EED0001),
+                                        ((2048, 2048), 0x5EED0000), ((777, 1313), 0x5EED0003)])
+def test_watershed_domain_parallel_on_tiles(cuda, orc, shape, seed):
+    """The domain-parallel flood (no serial fallback) is bit-exact on the
+    watershed inputs segmentNuclei produces."""
+    from nscale_gb300 import morphologic_operations as MO
+    nuclei, d2 = _pipeline_ws_inputs(orc, *shape, seed)
+    got = N(MO.watershed2(T(nuclei), T(d2), 8))
+    diag = _ws_diag()
+    np.testing.assert_array_equal(got, orc.watershed2(nuclei, d2, 8))
+    assert diag[0] == 0, f"fast path not taken (fallback code {diag[0]})"
+    assert diag[9] == 1  # a background flood event was resolved
+
+
+@pytest.mark.parametrize("conn", [4, 8])
+@pytest.mark.parametrize("const_colour", [False, True])
+def test_watershed_disc_pairs(cuda, orc, conn, const_colour):
+    from nscale_gb300 import morphologic_operations as MO
+    from nscale_gb300 import synth
+    m = synth.disc_pairs_mask(1024, 1024, seed=0x5EED0002)
+    d = orc.dist_transform(m)
+    distance = np.where(m > 0, -d, -np.finfo(np.float32).max).astype(np.float32)
+    d2 = orc.imhmin(distance, 1.0, 8)
+    bgr = synth.colorize_mask(m, seed=0x5EED0000)
+    if const_colour:
+        bgr = np.where(m[..., None] > 0, np.uint8(128), np.uint8(0)).astype(np.uint8)
+    got = N(MO.watershed2(T(bgr), T(d2), conn))
+    np.testing.assert_array_equal(got, orc.watershed2(bgr, d2, conn))
+    assert _ws_diag()[0] == 0
+
+
+def test_watershed_serial_entry(cuda, orc):
+    import ctypes as C
+    import torch
+    from nscale_gb300.context import get_context, ptr, stream_handle
+    nuclei, d2 = _pipeline_ws_inputs(orc, 256, 300, 0x5EED0004)
+    ctx = get_context(256, 300)
+    out = torch.empty((256, 300), dtype=torch.int32, device="cuda")
+    ctx.check(ctx.L.nsg_watershed_serial(ctx.h, ptr(T(nuclei)), ptr(T(d2)), ptr(out), 256, 300, 8, stream_handle()))
+    np.testing.assert_array_equal(N(out), orc.watershed2(nuclei, d2, 8))
+
+
+def test_watershed_adversarial_small(cuda, orc):
+    """Random colours (many black pixels) and random minima: whichever path the
+    flood takes (domain-parallel or its serial fallback), labels are exact."""
+    from nscale_gb300 import morphologic_operations as MO
+    rng = np.random.default_rng(7)
+    paths = {}
+    for it in range(150):
+        h, w = (int(v) for v in rng.integers(3, 48, size=2))
+        d2 = rng.integers(0, 6, size=(h, w)).astype(np.float32)
+        bgr = rng.integers(0, int(rng.integers(2, 256)), size=(h, w, 3)).astype(np.uint8)
+        bgr[rng.random((h, w)) < rng.random()] = 0
+        got = N(MO.watershed2(T(bgr), T(d2), 8 if it % 2 else 4))
+        paths[_ws_diag()[0]] = paths.get(_ws_diag()[0], 0) + 1
+        np.testing.assert_array_equal(got, orc.watershed2(bgr, d2, 8 if it % 2 else 4), err_msg=f"case {it}")
+    assert paths.get(0, 0) > 0
