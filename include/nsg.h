@@ -184,6 +184,18 @@ int nsg_segment_nuclei_host(nsg_context *ctx, const uint8_t *bgr_host, int rows,
                             int32_t *labels_host, uint8_t *mask_host, int *compcount, int32_t **bbox,
                             nsg_stream_t stream);
 
+/* Per-stage CUDA-event timing of segmentNuclei, in place of the reference's
+ * SimpleCSVLogger::logTimeSinceLastLog (UtilsLogger.h:85-183; stage names as
+ * HistologicalEntities.cpp logs them).  Enabling resets the accumulators;
+ * nsg_context_stage_times copies up to n accumulated milliseconds and returns
+ * the number of stages; nsg_stage_name gives stage i's name. */
+int nsg_context_set_timing(nsg_context *ctx, int on);
+int nsg_context_stage_times(nsg_context *ctx, double *ms_out, int n, long long *calls);
+const char *nsg_stage_name(int i);
+
+/* Number of CUDA kernels this library has launched in this process. */
+long long nsg_kernel_launches(void);
+
 void *nsg_alloc(size_t bytes);
 void nsg_free(void *p);
 

@@ -345,8 +345,11 @@ int exclusive_scan_i32(Ctx &c, const int32_t *in, int32_t *out, int64_t n, int32
     int nb = (int)((n + kScanTile - 1) / kScanTile);
     if (nb < 1) nb = 1;
     scan_tiles<<<nb, kScanThreads, 0, s>>>(in, out, n, c.ws.scan_tmp);
+    NSG_COUNT_LAUNCH();
     scan_sums<<<1, kScanThreads, 0, s>>>(c.ws.scan_tmp, nb, d_total);
+    NSG_COUNT_LAUNCH();
     scan_add<<<nb, 256, 0, s>>>(out, n, c.ws.scan_tmp);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
@@ -357,18 +360,25 @@ int ccl_u8(Ctx &c, const uint8_t *img, int32_t *parent, int rows, int cols, int 
     switch (mode) {
         case CCL_EQUAL:
             ccl_init<CCL_EQUAL><<<g, kB, 0, s>>>(img, parent, n);
+            NSG_COUNT_LAUNCH();
             ccl_merge<CCL_EQUAL><<<g, kB, 0, s>>>(img, parent, rows, cols, conn);
+            NSG_COUNT_LAUNCH();
             break;
         case CCL_NONZERO:
             ccl_init<CCL_NONZERO><<<g, kB, 0, s>>>(img, parent, n);
+            NSG_COUNT_LAUNCH();
             ccl_merge<CCL_NONZERO><<<g, kB, 0, s>>>(img, parent, rows, cols, conn);
+            NSG_COUNT_LAUNCH();
             break;
         default:
             ccl_init<CCL_NOT255><<<g, kB, 0, s>>>(img, parent, n);
+            NSG_COUNT_LAUNCH();
             ccl_merge<CCL_NOT255><<<g, kB, 0, s>>>(img, parent, rows, cols, conn);
+            NSG_COUNT_LAUNCH();
             break;
     }
     ccl_flatten<<<g, kB, 0, s>>>(parent, n);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
@@ -378,8 +388,11 @@ int ccl_f32_masked(Ctx &c, const float *val, const uint8_t *valid, int32_t *pare
     int64_t n = (int64_t)rows * cols;
     int g = blocks(c, n);
     cclf_init<<<g, kB, 0, s>>>(valid, parent, n);
+    NSG_COUNT_LAUNCH();
     cclf_merge<<<g, kB, 0, s>>>(val, valid, parent, rows, cols, conn);
+    NSG_COUNT_LAUNCH();
     ccl_flatten<<<g, kB, 0, s>>>(parent, n);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
@@ -394,7 +407,9 @@ int bwareaopen_dev(Ctx &c, const uint8_t *img, uint8_t *out, int rows, int cols,
     NSG_CUDA_TRY(c, cudaMemsetAsync(d_count, 0, sizeof(int), s));
     int g = blocks(c, n);
     area_count<<<g, kB, 0, s>>>(lab, area, n);
+    NSG_COUNT_LAUNCH();
     area_select<<<g, kB, 0, s>>>(lab, area, n, min_size, max_size, out, d_count);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
@@ -407,8 +422,11 @@ int recon_binary_dev(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t
     NSG_TRY(ccl_u8(c, mask, lab, rows, cols, conn, CCL_NONZERO, s));
     int g = blocks(c, n);
     zero_flags_at_roots<<<g, kB, 0, s>>>(lab, flag, n);
+    NSG_COUNT_LAUNCH();
     flag_seeds<<<g, kB, 0, s>>>(lab, marker, mask, flag, n);
+    NSG_COUNT_LAUNCH();
     select_recon<<<g, kB, 0, s>>>(lab, flag, marker, mask, out, n);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
@@ -420,8 +438,11 @@ int bwselect_dev(Ctx &c, const uint8_t *bw, const uint8_t *seeds, uint8_t *out, 
     NSG_TRY(ccl_u8(c, bw, lab, rows, cols, conn, CCL_NONZERO, s));
     int g = blocks(c, n);
     zero_flags_at_roots<<<g, kB, 0, s>>>(lab, flag, n);
+    NSG_COUNT_LAUNCH();
     flag_seeds<<<g, kB, 0, s>>>(lab, seeds, bw, flag, n);
+    NSG_COUNT_LAUNCH();
     select_bw<<<g, kB, 0, s>>>(lab, flag, bw, out, n);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
@@ -432,8 +453,11 @@ int fill_holes_dev(Ctx &c, const uint8_t *img, uint8_t *out, int rows, int cols,
     NSG_TRY(ccl_u8(c, img, lab, rows, cols, conn, CCL_NOT255, s));
     int g = blocks(c, n);
     zero_flags_at_roots<<<g, kB, 0, s>>>(lab, flag, n);
+    NSG_COUNT_LAUNCH();
     flag_border<<<blocks(c, 2 * (int64_t)rows + 2 * cols), kB, 0, s>>>(lab, flag, rows, cols);
+    NSG_COUNT_LAUNCH();
     select_fill<<<g, kB, 0, s>>>(lab, flag, out, n);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
@@ -449,11 +473,15 @@ int bbox_dev(Ctx &c, const int32_t *labels, int rows, int cols, int32_t *d_bbox,
     int *mnx = c.ws.i32[0], *mxx = c.ws.i32[1], *mny = c.ws.i32[2], *mxy = c.ws.i32[3], *pos = c.ws.i32[4];
     int g = blocks(c, n);
     bbox_init<<<g, kB, 0, s>>>(mnx, mxx, mny, mxy, labels, n);
+    NSG_COUNT_LAUNCH();
     bbox_accum<<<g, kB, 0, s>>>(labels, rows, cols, mnx, mxx, mny, mxy);
+    NSG_COUNT_LAUNCH();
     root_flags<<<g, kB, 0, s>>>(labels, pos, n);
+    NSG_COUNT_LAUNCH();
     NSG_TRY(exclusive_scan_i32(c, pos, pos, n, d_count, s));
     bbox_write<<<g, kB, 0, s>>>(labels, pos, n, d_count, mnx, mxx, mny, mxy, d_bbox, cap_ints,
                                 c.ws.ctrl + C_STATUS);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }

@@ -8,6 +8,8 @@
 
 namespace nsg {
 
+std::atomic<long long> g_kernel_launches{0};
+
 int sync_status(Ctx &c, cudaStream_t s) {
     NSG_CUDA_TRY(c, cudaMemcpyAsync(c.ws.h_ctrl, c.ws.ctrl + C_STATUS, sizeof(int), cudaMemcpyDeviceToHost, s));
     NSG_CUDA_TRY(c, cudaStreamSynchronize(s));
@@ -173,6 +175,8 @@ int nsg_context_set_spin_budget(nsg_context *h, long long it) {
 }
 
 void *nsg_alloc(size_t bytes) { return malloc(bytes ? bytes : 1); }
+
+long long nsg_kernel_launches(void) { return g_kernel_launches.load(); }
 void nsg_free(void *p) { free(p); }
 
 }  // extern "C"

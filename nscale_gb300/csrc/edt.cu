@@ -93,10 +93,12 @@ int dist_transform_dev(Ctx &c, const uint8_t *mask, float *dist, int rows, int c
     int *anyz = c.ws.ctrl + C_FLAG0;
     NSG_CUDA_TRY(c, cudaMemsetAsync(anyz, 0, sizeof(int), s));
     edt_cols<<<(cols + 127) / 128, 128, 0, s>>>(mask, g, rows, cols, anyz);
+    NSG_COUNT_LAUNCH();
     int64_t n = (int64_t)rows * cols;
     int64_t gb = (n + 255) / 256;
     if (gb > (int64_t)c.sm_count * 16) gb = (int64_t)c.sm_count * 16;
     edt_rows<<<(int)gb, 256, 0, s>>>(g, dist, rows, cols, anyz);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }

@@ -92,9 +92,11 @@ int imhmin_dev(Ctx &c, const float *img, float *out, int rows, int cols, float h
     int64_t n = (int64_t)rows * cols;
     float *mask = c.ws.f32[0], *marker = c.ws.f32[1];
     hmin_prep<<<blocks(c, n), kB, 0, s>>>(img, h, mask, marker, n);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     NSG_TRY(recon_f32(c, marker, mask, out, rows, cols, conn, s));
     negate<<<blocks(c, n), kB, 0, s>>>(out, n);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
@@ -108,14 +110,19 @@ int local_extrema_dev(Ctx &c, const float *img, uint8_t *out, int rows, int cols
     int *lab = c.ws.i32[0], *flag = c.ws.i32[1];
     int g = blocks(c, n);
     ext_prep<<<g, kB, 0, s>>>(img, minima, cim, marker, n);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     NSG_TRY(recon_f32(c, marker, cim, rec, rows, cols, conn, s));
     ext_cand<<<g, kB, 0, s>>>(marker, rec, cand, n);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     NSG_TRY(ccl_f32_masked(c, cim, cand, lab, rows, cols, conn, s));
     ext_zero_roots<<<g, kB, 0, s>>>(lab, flag, n);
+    NSG_COUNT_LAUNCH();
     ext_flag<<<g, kB, 0, s>>>(cim, lab, flag, rows, cols, conn);
+    NSG_COUNT_LAUNCH();
     ext_out<<<g, kB, 0, s>>>(lab, flag, out, n);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }

@@ -188,6 +188,7 @@ int morph_u8(Ctx &c, const uint8_t *in, uint8_t *out, int rows, int cols, const 
             chord_kernel<true><<<grid, kThreads, smem, s>>>(in, out, rows, cols, cs);
         else
             chord_kernel<false><<<grid, kThreads, smem, s>>>(in, out, rows, cols, cs);
+        NSG_COUNT_LAUNCH();
         NSG_LAUNCH_CHECK(c);
         return NSG_SUCCESS;
     }
@@ -212,6 +213,7 @@ int morph_u8(Ctx &c, const uint8_t *in, uint8_t *out, int rows, int cols, const 
         tap_kernel<true><<<grid, kThreads, smem, s>>>(in, out, rows, cols, d_ts);
     else
         tap_kernel<false><<<grid, kThreads, smem, s>>>(in, out, rows, cols, d_ts);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     // the host copy of `ts` must outlive the async copy
     NSG_CUDA_TRY(c, cudaStreamSynchronize(s));

@@ -5,11 +5,16 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <atomic>
 #include <string>
 
 #include "../../include/nsg.h"
 
 namespace nsg {
+
+// Number of kernels this library has launched (process-wide, monotone).
+extern std::atomic<long long> g_kernel_launches;
+#define NSG_COUNT_LAUNCH() (::nsg::g_kernel_launches.fetch_add(1, std::memory_order_relaxed))
 
 // Device status word bits reported by persistent / spinning kernels.
 enum DeviceStatus : int {
@@ -61,8 +66,22 @@ enum Ctrl : int {
     C_QSLOTS = 1024, // 3072 ints: generic small arrays
 };
 
+// Per-stage CUDA-event timing of segmentNuclei (the GPU analogue of the
+// reference's SimpleCSVLogger::logTimeSinceLastLog stage names).
+constexpr int kStages = 19;
+struct StageTimer {
+    bool on = false;
+    bool created = false;
+    cudaEvent_t ev[kStages + 2];
+    int stage[kStages + 2];
+    int nrec = 0;
+    double acc_ms[kStages] = {};
+    long long calls = 0;
+};
+
 struct Ctx {
     int device = 0;
+    StageTimer timer;
     int max_rows = 0, max_cols = 0;
     int64_t max_px = 0, max_pad = 0;
     void *arena = nullptr;

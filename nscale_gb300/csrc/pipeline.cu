@@ -64,6 +64,46 @@ int read_counts(Ctx &c, cudaStream_t s) {
     return NSG_SUCCESS;
 }
 
+const char *kStageNames[kStages] = {"background", "RBC", "open19", "reconToNuclei", "fillHoles1",
+                                   "areaThreshold1", "blobsGt45", "fillHoles2", "openBlobs", "30To1000",
+                                   "dilate", "distTransform", "imhmin", "watershed", "20To1000",
+                                   "fillHolesLast", "bwlabel2", "bounding_box", "other"};
+
+// timer: record the end of `stage` (the segment since the previous mark)
+void t_start(Ctx &c, cudaStream_t s) {
+    StageTimer &t = c.timer;
+    t.nrec = 0;
+    if (!t.on) return;
+    if (!t.created) {
+        for (int i = 0; i < kStages + 2; ++i) cudaEventCreate(&t.ev[i]);
+        t.created = true;
+    }
+    cudaEventRecord(t.ev[0], s);
+    t.stage[0] = -1;
+    t.nrec = 1;
+}
+void t_mark(Ctx &c, int stage, cudaStream_t s) {
+    StageTimer &t = c.timer;
+    if (!t.on || t.nrec == 0 || t.nrec >= kStages + 2) return;
+    cudaEventRecord(t.ev[t.nrec], s);
+    t.stage[t.nrec] = stage;
+    t.nrec++;
+}
+// after the stream has been synchronised
+void t_finish(Ctx &c, cudaStream_t s) {
+    StageTimer &t = c.timer;
+    if (!t.on || t.nrec < 2) return;
+    cudaEventSynchronize(t.ev[t.nrec - 1]);
+    for (int i = 1; i < t.nrec; ++i) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, t.ev[i - 1], t.ev[i]);
+        t.acc_ms[t.stage[i]] += ms;
+    }
+    t.calls++;
+    t.nrec = 0;
+    (void)s;
+}
+
 }  // namespace
 
 int segment_nuclei_dev(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int cols, const nsg_seg_params &p,
@@ -84,15 +124,25 @@ int segment_nuclei_dev(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int
     int *ctrl = c.ws.ctrl;
     const int g = blocks(c, n);
     auto fail_fill = [&](int status) -> int {
-        if (labels_out) fill_i32<<<g, kB, 0, s>>>(labels_out, -1, n);
+        if (labels_out) {
+            fill_i32<<<g, kB, 0, s>>>(labels_out, -1, n);
+            NSG_COUNT_LAUNCH();
+        }
         if (mask_out) cudaMemsetAsync(mask_out, 0, n, s);
         return status;
     };
     NSG_CUDA_TRY(c, cudaMemsetAsync(ctrl, 0, 8 * sizeof(int), s));
+    t_start(c, s);
+    struct Fin {
+        Ctx &c;
+        cudaStream_t s;
+        ~Fin() { t_finish(c, s); }
+    } fin_timer{c, s};
 
     // ---- plFindNucleusCandidates --------------------------------------------
     NSG_TRY(background_count(c, bgr, stride, rows, cols, p.blue, p.green, p.red, nullptr, c.ws.ctr64, s));
     NSG_TRY(front_rbc(c, bgr, stride, rows, cols, p.T1, p.T2, P[0], P[1], P[2], P[3], ctrl + C_COUNT0, s));
+    t_mark(c, 0, s);
     NSG_TRY(read_counts(c, s));
     {
         float ratio = (float)c.ws.h_ctr64[0] / (float)n;  // HE:125-126
@@ -102,54 +152,73 @@ int segment_nuclei_dev(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int
     // rbc = bwselect(bw2, bw1, 8) & imR2B (no seeds -> all zero, HE:73-79)
     NSG_TRY(bwselect_dev(c, P[2], P[1], P[4], rows, cols, 8, s));
     and_u8<<<g, kB, 0, s>>>(P[4], P[3], n);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
+    t_mark(c, 1, s);
     // rc_open = morphOpen(rc, disk19)
     uint8_t se19[361];
     disk19(se19);
     NSG_TRY(morph_u8(c, P[0], P[5], rows, cols, se19, 19, false, s));
     NSG_TRY(morph_u8(c, P[5], P[6], rows, cols, se19, 19, true, s));
+    t_mark(c, 2, s);
     // rc_recon = imreconstruct(rc_open, rc, reconConnectivity)
     NSG_TRY(recon_u8(c, P[6], P[0], P[7], rows, cols, p.reconConnectivity, s));
     // diffIm > G1, diffIm > G2
     NSG_TRY(diff_threshold(c, P[0], P[7], rows, cols, p.G1, p.G2, P[5], P[8], s));
+    t_mark(c, 3, s);
     // bw1 = imfillHoles(diffIm > G1, fillHolesConnectivity)
     NSG_TRY(fill_holes_dev(c, P[5], P[6], rows, cols, p.fillHolesConnectivity, s));
+    t_mark(c, 4, s);
     // bw1_t = bwareaopen2(bw1, minSize, maxSize, 8)
     NSG_TRY(bwareaopen_dev(c, P[6], P[7], rows, cols, p.minSize, p.maxSize, 8, ctrl + C_COUNT1, s));
+    t_mark(c, 5, s);
     NSG_TRY(read_counts(c, s));
     if (c.ws.h_ctrl[C_COUNT1] == 0) return fail_fill(NSG_NO_CANDIDATES_LEFT);
     // seg_norbc = bwselect(diffIm > G2, bw1_t, 8) & (rbc == 0)
     NSG_TRY(bwselect_dev(c, P[8], P[7], P[5], rows, cols, 8, s));
     NSG_TRY(and_not(c, P[5], P[4], n, s));
+    t_mark(c, 6, s);
 
     // ---- segmentNuclei body -----------------------------------------------------
     NSG_TRY(fill_holes_dev(c, P[5], P[6], rows, cols, 4, s));  // HE:494 (hard-coded 4)
+    t_mark(c, 7, s);
     NSG_TRY(morph_u8(c, P[6], P[7], rows, cols, kCross3, 3, false, s));
     NSG_TRY(morph_u8(c, P[7], P[8], rows, cols, kCross3, 3, true, s));  // seg_open
+    t_mark(c, 8, s);
 
     // ---- plSeparateNuclei ---------------------------------------------------------
     NSG_TRY(bwareaopen_dev(c, P[8], P[5], rows, cols, p.minSizePl, INT_MAX, 8, ctrl + C_COUNT2, s));
+    t_mark(c, 9, s);
     NSG_TRY(morph_u8(c, P[5], P[6], rows, cols, kCross3, 3, true, s));  // seg_big
+    t_mark(c, 10, s);
     NSG_TRY(dist_transform_dev(c, P[6], c.ws.p_f32[0], rows, cols, s));
     NSG_TRY(neg_dist_mask(c, c.ws.p_f32[0], P[6], n, c.ws.p_f32[1], s));
+    t_mark(c, 11, s);
     NSG_TRY(imhmin_dev(c, c.ws.p_f32[1], c.ws.p_f32[0], rows, cols, 1.0f, 8, s));  // HE:384 (hard-coded 8)
+    t_mark(c, 12, s);
     uint8_t *nuclei = (uint8_t *)c.ws.p_i32[0];
     NSG_TRY(mask_copy_bgr(c, bgr, stride, P[6], rows, cols, nuclei, s));
     NSG_TRY(watershed_dev(c, nuclei, c.ws.p_f32[0], c.ws.p_i32[1], rows, cols, p.watershedConnectivity, s));
     keep_ge0<<<g, kB, 0, s>>>(P[6], c.ws.p_i32[1], P[7], n);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
+    t_mark(c, 13, s);
 
     // ---- final area filter, fill, label, boxes ------------------------------------
     NSG_TRY(bwareaopen_dev(c, P[7], P[8], rows, cols, p.minSizeSeg, p.maxSizeSeg, 4, ctrl + C_COUNT3, s));
+    t_mark(c, 14, s);
     NSG_TRY(read_counts(c, s));
     if (c.ws.h_ctrl[C_COUNT3] == 0) return fail_fill(NSG_NO_CANDIDATES_LEFT);
     uint8_t *fin = mask_out ? mask_out : P[9];
     NSG_TRY(fill_holes_dev(c, P[8], fin, rows, cols, p.fillHolesConnectivity, s));
+    t_mark(c, 15, s);
     int32_t *labels = labels_out ? labels_out : c.ws.p_i32[0];
     NSG_TRY(bwlabel_dev(c, fin, labels, rows, cols, 8, s));
+    t_mark(c, 16, s);
     if (compcount || bbox) {
         int32_t *d_bbox = c.ws.p_i32[1];
         NSG_TRY(bbox_dev(c, labels, rows, cols, d_bbox, c.max_pad, ctrl + C_COUNT0, s));
+        t_mark(c, 17, s);
         NSG_TRY(read_counts(c, s));
         int cnt = c.ws.h_ctrl[C_COUNT0];
         if (compcount) *compcount = cnt;
@@ -223,6 +292,7 @@ int nsg_get_rbc(nsg_context *h, const uint8_t *bgr, int rows, int cols, double T
         NSG_TRY(bwselect_dev(c, bw2, bw1, rbc_out, rows, cols, 8, S(s)));
         int64_t n = (int64_t)rows * cols;
         and_u8<<<blocks(c, n), kB, 0, S(s)>>>(rbc_out, r2b, n);
+        NSG_COUNT_LAUNCH();
         NSG_LAUNCH_CHECK(c);
         return NSG_SUCCESS;
     });
@@ -420,6 +490,24 @@ int nsg_bounding_box(nsg_context *h, const int32_t *labels, int rows, int cols, 
     }
     return NSG_SUCCESS;
 }
+
+int nsg_context_set_timing(nsg_context *h, int on) {
+    if (!h) return NSG_ERR_ARG;
+    h->c.timer.on = on != 0;
+    for (int i = 0; i < kStages; ++i) h->c.timer.acc_ms[i] = 0.0;
+    h->c.timer.calls = 0;
+    return NSG_SUCCESS;
+}
+
+int nsg_context_stage_times(nsg_context *h, double *ms_out, int n, long long *calls) {
+    if (!h || !ms_out) return NSG_ERR_ARG;
+    int m = n < kStages ? n : kStages;
+    for (int i = 0; i < m; ++i) ms_out[i] = h->c.timer.acc_ms[i];
+    if (calls) *calls = h->c.timer.calls;
+    return kStages;
+}
+
+const char *nsg_stage_name(int i) { return (i >= 0 && i < kStages) ? kStageNames[i] : ""; }
 
 int nsg_segment_nuclei(nsg_context *h, const uint8_t *bgr, int rows, int cols, size_t row_stride_bytes,
                        const nsg_seg_params *p, int32_t *labels_out, uint8_t *mask_out, int *compcount,

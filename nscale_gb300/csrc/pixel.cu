@@ -131,6 +131,7 @@ int background_count(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int c
     int64_t chunks = (int64_t)((cols + 15) / 16) * rows;
     background_kernel<16><<<blocks_for(c, chunks), kBlock, 0, s>>>(bgr, stride, rows, cols, blue, green, red, mask,
                                                                    (unsigned long long *)d_count);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
@@ -141,6 +142,7 @@ int front_rbc(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int cols, do
     int64_t n = (int64_t)rows * cols;
     front_rbc_kernel<<<blocks_for(c, n), kBlock, 0, s>>>(bgr, stride, rows, cols, (float)T1, (float)T2, rc, bw1, bw2,
                                                          r2b, d_bw1_count);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
@@ -149,12 +151,14 @@ int diff_threshold(Ctx &c, const uint8_t *rc, const uint8_t *rec, int rows, int 
                    uint8_t *o2, cudaStream_t s) {
     int64_t n = (int64_t)rows * cols;
     diff_threshold_kernel<<<blocks_for(c, n), kBlock, 0, s>>>(rc, rec, n, G1, G2, o1, o2);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
 
 int and_not(Ctx &c, uint8_t *io, const uint8_t *nm, int64_t n, cudaStream_t s) {
     and_not_kernel<<<blocks_for(c, n), kBlock, 0, s>>>(io, nm, n);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
@@ -163,18 +167,21 @@ int mask_copy_bgr(Ctx &c, const uint8_t *bgr, int64_t stride, const uint8_t *m, 
                   cudaStream_t s) {
     int64_t n = (int64_t)rows * cols;
     mask_copy_bgr_kernel<<<blocks_for(c, n), kBlock, 0, s>>>(bgr, stride, m, rows, cols, out);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
 
 int neg_dist_mask(Ctx &c, const float *d, const uint8_t *m, int64_t n, float *out, cudaStream_t s) {
     neg_dist_mask_kernel<<<blocks_for(c, n), kBlock, 0, s>>>(d, m, n, out);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
 
 int invert_u8_dev(Ctx &c, const uint8_t *in, uint8_t *out, int64_t n, cudaStream_t s) {
     invert_kernel<<<blocks_for(c, n), kBlock, 0, s>>>(in, out, n);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }

@@ -389,8 +389,10 @@ int run_recon(Ctx &c, const T *marker, const T *mask, T *out, int rows, int cols
         init_min_u8<<<blocks, 256, 0, s>>>((const uint8_t *)marker, (const uint8_t *)mask, (uint8_t *)out, n);
     else
         init_min_f32<<<blocks, 256, 0, s>>>((const float *)marker, (const float *)mask, (float *)out, n);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     init_queue<<<(qcap + 255) / 256, 256, 0, s>>>(state, queue, qcap, ntiles, c.ws.ctrl);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     Queue q;
     q.state = state;
@@ -411,6 +413,7 @@ int run_recon(Ctx &c, const T *marker, const T *mask, T *out, int rows, int cols
     int need = (ntiles + WARPS - 1) / WARPS;
     if (grid > need) grid = need;
     kfn<<<grid, WARPS * 32, smem, s>>>(mask, out, rows, cols, conn, tiles_x, tiles_y, q);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }

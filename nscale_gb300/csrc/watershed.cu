@@ -71,9 +71,11 @@ int watershed_dev(Ctx &c, const uint8_t *bgr, const float *img, int32_t *out, in
     NSG_TRY(bwlabel_dev(c, minima, labels, rows, cols, conn, s));
     int64_t np = (int64_t)(rows + 2) * (cols + 2);
     ws_pack<<<blocks(c, np), 256, 0, s>>>(labels, bgr, rows, cols, mk, colp);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     NSG_TRY(pws_flood(c, mk, colp, outp, rows + 2, cols + 2, s));
     ws_border_crop<<<blocks(c, (int64_t)rows * cols), 256, 0, s>>>(outp, rows, cols, out);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
@@ -89,9 +91,11 @@ int watershed_serial_dev(Ctx &c, const uint8_t *bgr, const float *img, int32_t *
     NSG_TRY(bwlabel_dev(c, minima, labels, rows, cols, conn, s));
     int64_t np = (int64_t)(rows + 2) * (cols + 2);
     ws_pack<<<blocks(c, np), 256, 0, s>>>(labels, bgr, rows, cols, mk, colp);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     NSG_TRY(ws_flood_serial_launch(c, mk, colp, outp, rows + 2, cols + 2, false, s));
     ws_border_crop<<<blocks(c, (int64_t)rows * cols), 256, 0, s>>>(outp, rows, cols, out);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }

@@ -1190,10 +1190,12 @@ int ws_flood_serial_launch(Ctx &c, const int *mk, const uint32_t *col, int *outp
     int *next = (int *)c.ws.wsb;
     if (conditional) {
         k_copy_if<<<blocks(c, n), kB, 0, s>>>(mk, outp, n, flag);
+        NSG_COUNT_LAUNCH();
     } else {
         cudaMemcpyAsync(outp, mk, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, s);
     }
     k_serial<<<1, 32, 0, s>>>(outp, col, next, H, W, c.spin_budget * 64, c.ws.ctrl + C_STATUS, flag);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
@@ -1219,46 +1221,69 @@ int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int 
     const int g = blocks(c, n);
     NSG_CUDA_TRY(c, cudaMemsetAsync(a.ctl, 0, 64 * sizeof(int), s));
     k_classify<<<g, kB, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     NSG_TRY(ccl_u8(c, a.fgimg, a.domroot, H, W, 4, CCL_NONZERO, s));
     k_roots<<<g, kB, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     NSG_TRY(exclusive_scan_i32(c, a.isroot, a.rank, n, a.ctl + W_ND, s));
     k_domains<<<g, kB, 0, s>>>(a, a.ctl + W_ND);
+    NSG_COUNT_LAUNCH();
     NSG_TRY(exclusive_scan_i32(c, a.dsize, a.doff, n, nullptr, s));
     NSG_LAUNCH_CHECK(c);
     // P1: one thread per domain (the grid covers the largest possible count)
     const int gd = c.sm_count * 32;  // per-domain kernels: grid-stride over the domain count
     k_phase1<<<gd, 64, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     // P2
     k_true_dummies<<<g, kB, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     k_candidates<<<g, kB, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     k_first_event<<<1, 1024, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     k_cuts<<<gd / 4, 256, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     k_state<<<g, kB, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     k_event_label<<<1, 32, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     k_bfs<<<1, 1024, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     k_shells<<<g, kB, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     uint8_t *pimg = a.fgimg;  // reuse: the domain image is no longer needed
     k_pocket_img<<<g, kB, 0, s>>>(a, pimg);
+    NSG_COUNT_LAUNCH();
     NSG_TRY(ccl_u8(c, pimg, a.proot, H, W, 4, CCL_NONZERO, s));
     int *powner = a.claim;  // BFS claims are no longer needed
     NSG_CUDA_TRY(c, cudaMemsetAsync(powner, 0xff, sizeof(int) * (size_t)n, s));
     k_pocket_owner<<<g, kB, 0, s>>>(a, powner);
+    NSG_COUNT_LAUNCH();
     k_shell_unions<<<g, kB, 0, s>>>(a, powner);
+    NSG_COUNT_LAUNCH();
     k_sup_flatten<<<g, kB, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     k_groups<<<g, kB, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     NSG_TRY(exclusive_scan_i32(c, a.mcount, a.moff, n, nullptr, s));
     k_groups2<<<g, kB, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     k_inj_count<<<g, kB, 0, s>>>(a, 0);
+    NSG_COUNT_LAUNCH();
     NSG_TRY(exclusive_scan_i32(c, a.icount, a.ioff, n, nullptr, s));
     k_inj_count<<<g, kB, 0, s>>>(a, 1);
+    NSG_COUNT_LAUNCH();
     k_reset_owned_u<<<g, kB, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     k_phase3<<<gd, 64, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     k_assemble<<<g, kB, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     // exact serial flood when a fast-path condition failed
     return ws_flood_serial_launch(c, mk, col, outp, H, W, true, s);

@@ -252,7 +252,7 @@ def test_watershed_disc_pairs(cuda, orc, conn, const_colour):
     d2 = orc.imhmin(distance, 1.0, 8)
     bgr = synth.colorize_mask(m, seed=0x5EED0000)
     if const_colour:
-        bgr = np.where(m[..., None] > 0, np.uint8(128), np.uint8(0)).astype(np.uint8)
+        bgr = np.repeat(np.where(m[..., None] > 0, 128, 0).astype(np.uint8), 3, axis=2)
     got = N(MO.watershed2(T(bgr), T(d2), conn))
     np.testing.assert_array_equal(got, orc.watershed2(bgr, d2, conn))
     assert _ws_diag()[0] == 0
@@ -265,7 +265,8 @@ def test_watershed_serial_entry(cuda, orc):
     nuclei, d2 = _pipeline_ws_inputs(orc, 256, 300, 0x5EED0004)
     ctx = get_context(256, 300)
     out = torch.empty((256, 300), dtype=torch.int32, device="cuda")
-    ctx.check(ctx.L.nsg_watershed_serial(ctx.h, ptr(T(nuclei)), ptr(T(d2)), ptr(out), 256, 300, 8, stream_handle()))
+    tn, td = T(nuclei), T(d2)  # keep the device buffers alive across the call
+    ctx.check(ctx.L.nsg_watershed_serial(ctx.h, ptr(tn), ptr(td), ptr(out), 256, 300, 8, stream_handle()))
     np.testing.assert_array_equal(N(out), orc.watershed2(nuclei, d2, 8))
 
 
