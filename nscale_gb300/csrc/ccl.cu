@@ -109,6 +109,124 @@ __global__ void ccl_flatten(int *parent, int64_t n) {
     }
 }
 
+// ---- block-local union-find ------------------------------------------------
+// A 32x32 tile is labelled in shared memory (union by atomicMin on local
+// indices, so local roots are the tile's minimum raster index of each piece,
+// which is also the minimum global index); then only pixel pairs that cross a
+// tile border are united in global memory.
+constexpr int LT = 32;
+
+struct PredU8 {
+    const uint8_t *img;
+    int mode;
+    __device__ __forceinline__ bool fg(int64_t i) const {
+        uint8_t v = img[i];
+        return mode == CCL_NOT255 ? v != 255 : v != 0;
+    }
+    __device__ __forceinline__ bool joins(int64_t i, int64_t j) const {
+        uint8_t a = img[i], b = img[j];
+        if (mode == CCL_EQUAL) return a == b && a != 0;
+        if (mode == CCL_NONZERO) return a != 0 && b != 0;
+        return a != 255 && b != 255;
+    }
+};
+struct PredF32 {
+    const float *val;
+    const uint8_t *valid;
+    __device__ __forceinline__ bool fg(int64_t i) const { return valid[i] != 0; }
+    __device__ __forceinline__ bool joins(int64_t i, int64_t j) const {
+        return valid[i] && valid[j] && val[i] == val[j];
+    }
+};
+
+__device__ __forceinline__ int lfind(int *l, int x) {
+    int p = l[x];
+    while (p != x) {
+        int gp = l[p];
+        l[x] = gp;  // halving in shared memory
+        x = p;
+        p = gp;
+    }
+    return x;
+}
+__device__ __forceinline__ void lunite(int *l, int a, int b) {
+    for (;;) {
+        a = lfind(l, a);
+        b = lfind(l, b);
+        if (a == b) return;
+        if (a < b) {
+            int t = a;
+            a = b;
+            b = t;
+        }
+        int old = atomicMin(l + a, b);
+        if (old == a) return;
+        a = old;
+    }
+}
+
+template <typename Pred>
+__global__ void __launch_bounds__(256) ccl_local(Pred pr, int *__restrict__ parent, int rows, int cols, int conn) {
+    __shared__ int l[LT * LT];
+    const int x0 = blockIdx.x * LT, y0 = blockIdx.y * LT;
+    const int tx = threadIdx.x & 31, tyb = threadIdx.x >> 5;  // 8 row groups
+    // init
+    for (int ty = tyb; ty < LT; ty += 8) {
+        int y = y0 + ty, x = x0 + tx, li = ty * LT + tx;
+        bool f = (y < rows && x < cols) && pr.fg((int64_t)y * cols + x);
+        l[li] = f ? li : -1;
+    }
+    __syncthreads();
+    for (int ty = tyb; ty < LT; ty += 8) {
+        int y = y0 + ty, x = x0 + tx, li = ty * LT + tx;
+        if (l[li] < 0) continue;
+        int64_t i = (int64_t)y * cols + x;
+        if (tx > 0 && pr.joins(i, i - 1)) lunite(l, li, li - 1);
+        if (ty > 0) {
+            int64_t u = i - cols;
+            if (pr.joins(i, u)) lunite(l, li, li - LT);
+            if (conn == 8) {
+                if (tx > 0 && pr.joins(i, u - 1)) lunite(l, li, li - LT - 1);
+                if (tx < LT - 1 && x < cols - 1 && pr.joins(i, u + 1)) lunite(l, li, li - LT + 1);
+            }
+        }
+    }
+    __syncthreads();
+    for (int ty = tyb; ty < LT; ty += 8) {
+        int y = y0 + ty, x = x0 + tx, li = ty * LT + tx;
+        if (y >= rows || x >= cols) continue;
+        int r = l[li];
+        if (r >= 0) {
+            while (l[r] != r) r = l[r];
+            r = (y0 + r / LT) * cols + (x0 + r % LT);
+        }
+        parent[(int64_t)y * cols + x] = r;
+    }
+}
+
+// unions of neighbour pairs that cross a tile border (backward neighbours:
+// left, up, up-left, up-right, the pairs ConnComponents::label visits)
+template <typename Pred>
+__global__ void ccl_border(Pred pr, int *parent, int rows, int cols, int conn) {
+    int64_t n = (int64_t)rows * cols;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int y = (int)(i / cols), x = (int)(i - (int64_t)y * cols);
+        int bx = x & (LT - 1), by = y & (LT - 1);
+        if (bx != 0 && by != 0 && bx != LT - 1) continue;
+        if (!pr.fg(i)) continue;
+        if (x > 0 && bx == 0 && pr.joins(i, i - 1)) unite(parent, (int)i, (int)(i - 1));
+        if (y > 0) {
+            int64_t u = i - cols;
+            if (by == 0 && pr.joins(i, u)) unite(parent, (int)i, (int)u);
+            if (conn == 8) {
+                if (x > 0 && (bx == 0 || by == 0) && pr.joins(i, u - 1)) unite(parent, (int)i, (int)(u - 1));
+                if (x < cols - 1 && (bx == LT - 1 || by == 0) && pr.joins(i, u + 1))
+                    unite(parent, (int)i, (int)(u + 1));
+            }
+        }
+    }
+}
+
 // float plateaus among valid pixels (local extrema floods)
 __global__ void cclf_init(const uint8_t *__restrict__ valid, int *__restrict__ parent, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -356,28 +474,13 @@ int exclusive_scan_i32(Ctx &c, const int32_t *in, int32_t *out, int64_t n, int32
 
 int ccl_u8(Ctx &c, const uint8_t *img, int32_t *parent, int rows, int cols, int conn, int mode, cudaStream_t s) {
     int64_t n = (int64_t)rows * cols;
-    int g = blocks(c, n);
-    switch (mode) {
-        case CCL_EQUAL:
-            ccl_init<CCL_EQUAL><<<g, kB, 0, s>>>(img, parent, n);
-            NSG_COUNT_LAUNCH();
-            ccl_merge<CCL_EQUAL><<<g, kB, 0, s>>>(img, parent, rows, cols, conn);
-            NSG_COUNT_LAUNCH();
-            break;
-        case CCL_NONZERO:
-            ccl_init<CCL_NONZERO><<<g, kB, 0, s>>>(img, parent, n);
-            NSG_COUNT_LAUNCH();
-            ccl_merge<CCL_NONZERO><<<g, kB, 0, s>>>(img, parent, rows, cols, conn);
-            NSG_COUNT_LAUNCH();
-            break;
-        default:
-            ccl_init<CCL_NOT255><<<g, kB, 0, s>>>(img, parent, n);
-            NSG_COUNT_LAUNCH();
-            ccl_merge<CCL_NOT255><<<g, kB, 0, s>>>(img, parent, rows, cols, conn);
-            NSG_COUNT_LAUNCH();
-            break;
-    }
-    ccl_flatten<<<g, kB, 0, s>>>(parent, n);
+    PredU8 pr{img, mode};
+    dim3 grid((cols + LT - 1) / LT, (rows + LT - 1) / LT);
+    ccl_local<PredU8><<<grid, 256, 0, s>>>(pr, parent, rows, cols, conn);
+    NSG_COUNT_LAUNCH();
+    ccl_border<PredU8><<<blocks(c, n), kB, 0, s>>>(pr, parent, rows, cols, conn);
+    NSG_COUNT_LAUNCH();
+    ccl_flatten<<<blocks(c, n), kB, 0, s>>>(parent, n);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
@@ -386,12 +489,13 @@ int ccl_u8(Ctx &c, const uint8_t *img, int32_t *parent, int rows, int cols, int 
 int ccl_f32_masked(Ctx &c, const float *val, const uint8_t *valid, int32_t *parent, int rows, int cols, int conn,
                    cudaStream_t s) {
     int64_t n = (int64_t)rows * cols;
-    int g = blocks(c, n);
-    cclf_init<<<g, kB, 0, s>>>(valid, parent, n);
+    PredF32 pr{val, valid};
+    dim3 grid((cols + LT - 1) / LT, (rows + LT - 1) / LT);
+    ccl_local<PredF32><<<grid, 256, 0, s>>>(pr, parent, rows, cols, conn);
     NSG_COUNT_LAUNCH();
-    cclf_merge<<<g, kB, 0, s>>>(val, valid, parent, rows, cols, conn);
+    ccl_border<PredF32><<<blocks(c, n), kB, 0, s>>>(pr, parent, rows, cols, conn);
     NSG_COUNT_LAUNCH();
-    ccl_flatten<<<g, kB, 0, s>>>(parent, n);
+    ccl_flatten<<<blocks(c, n), kB, 0, s>>>(parent, n);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;

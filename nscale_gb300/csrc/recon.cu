@@ -34,19 +34,6 @@ namespace {
 
 constexpr int TW = 64;  // tile width (2 pixels per lane)
 
-template <typename T>
-struct Lim;
-template <>
-struct Lim<uint8_t> {
-    __device__ static uint8_t lo() { return 0; }
-    __device__ static uint8_t hi() { return 255; }
-};
-template <>
-struct Lim<float> {
-    __device__ static float lo() { return -INFINITY; }
-    __device__ static float hi() { return INFINITY; }
-};
-
 // std::max / std::min as the reference writes them
 template <typename T>
 __device__ __forceinline__ T smax(T a, T b) {
@@ -369,6 +356,289 @@ __global__ void __launch_bounds__(WARPS * 32) recon_persistent(const T *__restri
     }
 }
 
+// ---------------------------------------------------------------------------
+// CTA-per-tile variant: one CTA (8 warps) owns a TW x TH tile.  Row phases
+// scan every row of the tile in parallel (one warp per row at a time, PX
+// pixels per lane, clamp-function prefix scans left->right then right->left,
+// vertical and diagonal neighbours taken from the current tile); column
+// phases do the same down and up the columns.  Phases alternate until a
+// whole phase pair changes nothing: then every pixel satisfies the 8- (or 4-)
+// neighbour fixed-point equation inside the tile.  Concurrent reads of rows
+// other warps are updating are benign: values only grow and stay below the
+// fixed point.
+template <typename T>
+__device__ __forceinline__ T ident_lo();
+template <>
+__device__ __forceinline__ uint8_t ident_lo<uint8_t>() { return 0; }
+template <>
+__device__ __forceinline__ float ident_lo<float>() { return -INFINITY; }
+template <typename T>
+__device__ __forceinline__ T ident_hi();
+template <>
+__device__ __forceinline__ uint8_t ident_hi<uint8_t>() { return 255; }
+template <>
+__device__ __forceinline__ float ident_hi<float>() { return INFINITY; }
+
+template <typename T, int TW, int TH, int P>
+struct TileSmem {
+    static constexpr int OW = P;  // row pitch of the halo tile (elements)
+    T o[(TH + 2) * P];
+    T m[TH * TW];
+    int edges;
+    int changed;
+    int tile;
+    int again;
+};
+
+// One line (row or column) of N = 32 * K pixels: forward then backward
+// clamp scans.  get(i) / put(i, v) address pixel i of the line (i = lane*K+k),
+// `lo`/`hi` are the per-pixel clamp bounds after the cross-line step, `first`
+// and `last` the values just outside the line.
+template <typename T, int K>
+__device__ __forceinline__ void line_scan(T (&lo)[K], T (&hi)[K], T first, T last, T (&res)[K]) {
+    const int lane = threadIdx.x & 31;
+    // forward: F = f_{K-1} o ... o f_0
+    T FL = lo[0], FH = hi[0];
+#pragma unroll
+    for (int k = 1; k < K; ++k) {
+        T nl = clampv(FL, lo[k], hi[k]), nh = clampv(FH, lo[k], hi[k]);
+        FL = nl;
+        FH = nh;
+    }
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        T pl = shfl_up(FL, d), ph = shfl_up(FH, d);
+        if (lane >= d) {
+            T nl = clampv(pl, FL, FH), nh = clampv(ph, FL, FH);
+            FL = nl;
+            FH = nh;
+        }
+    }
+    T el = shfl_up(FL, 1), eh = shfl_up(FH, 1);
+    T y = lane == 0 ? first : clampv(first, el, eh);
+    T v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        y = clampv(y, lo[k], hi[k]);
+        v[k] = y;
+    }
+    // backward on the forward result: g_k(y) = clamp(y, v_k, hi_k)
+    T BL = v[K - 1], BH = hi[K - 1];
+    if (hi[K - 1] == (T)0 && lo[K - 1] == (T)0) BL = (T)0;
+#pragma unroll
+    for (int k = K - 2; k >= 0; --k) {
+        T l2 = (hi[k] == (T)0 && lo[k] == (T)0) ? (T)0 : v[k];
+        T nl = clampv(BL, l2, hi[k]), nh = clampv(BH, l2, hi[k]);
+        BL = nl;
+        BH = nh;
+    }
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        T pl = shfl_down(BL, d), ph = shfl_down(BH, d);
+        if (lane + d < 32) {
+            T nl = clampv(pl, BL, BH), nh = clampv(ph, BL, BH);
+            BL = nl;
+            BH = nh;
+        }
+    }
+    el = shfl_down(BL, 1);
+    eh = shfl_down(BH, 1);
+    y = lane == 31 ? last : clampv(last, el, eh);
+#pragma unroll
+    for (int k = K - 1; k >= 0; --k) {
+        T l2 = (hi[k] == (T)0 && lo[k] == (T)0) ? (T)0 : v[k];
+        y = clampv(y, l2, hi[k]);
+        res[k] = y;
+    }
+}
+
+template <typename T, int TW, int TH, int P>
+__device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, int cols, bool conn8, int tx, int ty,
+                                 TileSmem<T, TW, TH, P> &sm) {
+    constexpr int NW = 8;
+    constexpr int KX = TW / 32, KY = TH / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int y0 = ty * TH, x0 = tx * TW;
+    T *o = sm.o;
+    // load tile + halo (image ring = 0) and the mask
+    for (int i = threadIdx.x; i < (TH + 2) * (TW + 2); i += NW * 32) {
+        int r = i / (TW + 2), cc = i - r * (TW + 2);
+        int y = y0 - 1 + r, x = x0 - 1 + cc;
+        o[r * P + cc] = (y >= 0 && y < rows && x >= 0 && x < cols) ? ldcg(out + (int64_t)y * cols + x) : (T)0;
+    }
+    for (int i = threadIdx.x; i < TH * TW; i += NW * 32) {
+        int r = i / TW, cc = i - r * TW;
+        int y = y0 + r, x = x0 + cc;
+        sm.m[i] = (y < rows && x < cols) ? __ldg(mask + (int64_t)y * cols + x) : (T)0;
+    }
+    if (threadIdx.x == 0) sm.edges = 0;
+    __syncthreads();
+    unsigned my_edges = 0;
+    const int vr = rows - y0, vc = cols - x0;  // valid extent of this tile
+    for (int it = 0; it < 1024; ++it) {
+        bool ch = false;
+        // ---- row phase
+        for (int r = warp; r < TH; r += NW) {
+            T *row = o + (r + 1) * P + 1;
+            const T *up = row - P, *dn = row + P;
+            T lo[KX], hi[KX], cur[KX], res[KX];
+#pragma unroll
+            for (int k = 0; k < KX; ++k) {
+                int x = lane * KX + k;
+                cur[k] = row[x];
+                T w = smax(cur[k], smax(up[x], dn[x]));
+                if (conn8) w = smax(w, smax(smax(up[x - 1], up[x + 1]), smax(dn[x - 1], dn[x + 1])));
+                T mk = sm.m[r * TW + x];
+                bool in = r < vr && x < vc;
+                lo[k] = in ? smin(w, mk) : (T)0;
+                hi[k] = in ? mk : (T)0;
+            }
+            line_scan<T, KX>(lo, hi, row[-1], row[TW], res);
+#pragma unroll
+            for (int k = 0; k < KX; ++k) {
+                int x = lane * KX + k;
+                if (!(res[k] == cur[k])) {
+                    row[x] = res[k];
+                    ch = true;
+                    if (r == 0) my_edges |= 1u;
+                    if (r == TH - 1) my_edges |= 2u;
+                    if (x == 0) my_edges |= 4u;
+                    if (x == TW - 1) my_edges |= 8u;
+                }
+            }
+        }
+        __syncthreads();
+        // ---- column phase
+        for (int cidx = warp; cidx < TW; cidx += NW) {
+            T lo[KY], hi[KY], cur[KY], res[KY];
+#pragma unroll
+            for (int k = 0; k < KY; ++k) {
+                int y = lane * KY + k;
+                T *p = o + (y + 1) * P + (cidx + 1);
+                cur[k] = p[0];
+                T w = smax(cur[k], smax(p[-1], p[1]));
+                if (conn8) w = smax(w, smax(smax(p[-P - 1], p[-P + 1]), smax(p[P - 1], p[P + 1])));
+                T mk = sm.m[y * TW + cidx];
+                bool in = y < vr && cidx < vc;
+                lo[k] = in ? smin(w, mk) : (T)0;
+                hi[k] = in ? mk : (T)0;
+            }
+            line_scan<T, KY>(lo, hi, o[cidx + 1], o[(TH + 1) * P + cidx + 1], res);
+#pragma unroll
+            for (int k = 0; k < KY; ++k) {
+                int y = lane * KY + k;
+                if (!(res[k] == cur[k])) {
+                    o[(y + 1) * P + cidx + 1] = res[k];
+                    ch = true;
+                    if (y == 0) my_edges |= 1u;
+                    if (y == TH - 1) my_edges |= 2u;
+                    if (cidx == 0) my_edges |= 4u;
+                    if (cidx == TW - 1) my_edges |= 8u;
+                }
+            }
+        }
+        if (!__syncthreads_or(ch)) break;
+        if (it == 1023) my_edges |= 16u;  // not stable yet: process again later
+    }
+    if (my_edges) atomicOr(&sm.edges, (int)my_edges);
+    // write back
+    for (int i = threadIdx.x; i < TH * TW; i += NW * 32) {
+        int r = i / TW, cc = i - r * TW;
+        int y = y0 + r, x = x0 + cc;
+        if (y < rows && x < cols) out[(int64_t)y * cols + x] = o[(r + 1) * P + cc + 1];
+    }
+    __threadfence();
+    __syncthreads();
+}
+
+template <typename T, int TW, int TH, int P>
+__global__ void __launch_bounds__(256) recon_cta(const T *__restrict__ mask, T *out, int rows, int cols, int conn,
+                                                 int tiles_x, int tiles_y, Queue q) {
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    TileSmem<T, TW, TH, P> &sm = *reinterpret_cast<TileSmem<T, TW, TH, P> *>(sm_raw);
+    const bool conn8 = conn == 8;
+    for (;;) {
+        if (threadIdx.x == 0) sm.tile = q_pop(q);
+        __syncthreads();
+        const int t = sm.tile;
+        __syncthreads();
+        if (t < 0) break;
+        __threadfence();
+        for (;;) {
+            const int tx = t % tiles_x, ty = t / tiles_x;
+            cta_process_tile<T, TW, TH, P>(mask, out, rows, cols, conn8, tx, ty, sm);
+            if (threadIdx.x == 0) {
+                unsigned edges = (unsigned)sm.edges;
+                if (edges & 16u) q_push(q, t);
+                if (edges & 1u && ty > 0) q_push(q, t - tiles_x);
+                if (edges & 2u && ty + 1 < tiles_y) q_push(q, t + tiles_x);
+                if (edges & 4u && tx > 0) q_push(q, t - 1);
+                if (edges & 8u && tx + 1 < tiles_x) q_push(q, t + 1);
+                if (conn8) {
+                    if ((edges & 5u) == 5u && ty > 0 && tx > 0) q_push(q, t - tiles_x - 1);
+                    if ((edges & 9u) == 9u && ty > 0 && tx + 1 < tiles_x) q_push(q, t - tiles_x + 1);
+                    if ((edges & 6u) == 6u && ty + 1 < tiles_y && tx > 0) q_push(q, t + tiles_x - 1);
+                    if ((edges & 10u) == 10u && ty + 1 < tiles_y && tx + 1 < tiles_x) q_push(q, t + tiles_x + 1);
+                }
+                sm.again = q_finish(q, t);
+            }
+            __syncthreads();
+            const int again = sm.again;
+            __syncthreads();
+            if (!again) break;
+            __threadfence();
+        }
+    }
+}
+
+template <typename T, int TW, int TH, int P>
+int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int cols, int conn, cudaStream_t s) {
+    NSG_TRY(check_dims(c, rows, cols));
+    NSG_TRY(check_conn(c, conn));
+    const int64_t n = (int64_t)rows * cols;
+    const int tiles_x = (cols + TW - 1) / TW, tiles_y = (rows + TH - 1) / TH;
+    const int ntiles = tiles_x * tiles_y;
+    const int qcap = 2 * ntiles;
+    int *state = c.ws.i32[5];
+    int *queue = state + ntiles;
+    if ((int64_t)ntiles + qcap > c.max_pad) {
+        c.last_error = "tile queue does not fit";
+        return NSG_ERR_OOM;
+    }
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > c.sm_count * 16) blocks = c.sm_count * 16;
+    if (sizeof(T) == 1)
+        init_min_u8<<<blocks, 256, 0, s>>>((const uint8_t *)marker, (const uint8_t *)mask, (uint8_t *)out, n);
+    else
+        init_min_f32<<<blocks, 256, 0, s>>>((const float *)marker, (const float *)mask, (float *)out, n);
+    NSG_COUNT_LAUNCH();
+    NSG_LAUNCH_CHECK(c);
+    init_queue<<<(qcap + 255) / 256, 256, 0, s>>>(state, queue, qcap, ntiles, c.ws.ctrl);
+    NSG_COUNT_LAUNCH();
+    NSG_LAUNCH_CHECK(c);
+    Queue q;
+    q.state = state;
+    q.queue = queue;
+    q.qcap = qcap;
+    q.head = c.ws.ctrl + C_QHEAD;
+    q.tail = c.ws.ctrl + C_QTAIL;
+    q.outstanding = c.ws.ctrl + C_QPEND;
+    q.status = c.ws.ctrl + C_STATUS;
+    q.budget = c.spin_budget;
+    const size_t smem = sizeof(TileSmem<T, TW, TH, P>);
+    auto kfn = recon_cta<T, TW, TH, P>;
+    NSG_CUDA_TRY(c, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    NSG_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, 256, smem));
+    if (per_sm < 1) per_sm = 1;
+    int grid = c.sm_count * per_sm;
+    if (grid > ntiles) grid = ntiles;
+    kfn<<<grid, 256, smem, s>>>(mask, out, rows, cols, conn, tiles_x, tiles_y, q);
+    NSG_COUNT_LAUNCH();
+    NSG_LAUNCH_CHECK(c);
+    return NSG_SUCCESS;
+}
+
 template <typename T, int TH, int WARPS>
 int run_recon(Ctx &c, const T *marker, const T *mask, T *out, int rows, int cols, int conn, cudaStream_t s) {
     NSG_TRY(check_dims(c, rows, cols));
@@ -422,11 +692,21 @@ int run_recon(Ctx &c, const T *marker, const T *mask, T *out, int rows, int cols
 
 int recon_u8(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t *out, int rows, int cols, int conn,
              cudaStream_t s) {
-    return run_recon<uint8_t, 64, 4>(c, marker, mask, out, rows, cols, conn, s);
+    return run_recon_cta<uint8_t, 128, 128, 132>(c, marker, mask, out, rows, cols, conn, s);
 }
 
 int recon_f32(Ctx &c, const float *marker, const float *mask, float *out, int rows, int cols, int conn,
               cudaStream_t s) {
+    return run_recon_cta<float, 64, 64, 67>(c, marker, mask, out, rows, cols, conn, s);
+}
+
+// the warp-per-tile variant (kept for comparison)
+int recon_u8_warp(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t *out, int rows, int cols, int conn,
+                  cudaStream_t s) {
+    return run_recon<uint8_t, 64, 4>(c, marker, mask, out, rows, cols, conn, s);
+}
+int recon_f32_warp(Ctx &c, const float *marker, const float *mask, float *out, int rows, int cols, int conn,
+                   cudaStream_t s) {
     return run_recon<float, 32, 4>(c, marker, mask, out, rows, cols, conn, s);
 }
 
