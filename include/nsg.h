@@ -113,6 +113,24 @@ int nsg_imreconstruct_binary_u8(nsg_context *ctx, const uint8_t *marker, const u
 /* nscale::imfillHoles<unsigned char>(img, binary=true, conn) (MorphologicOperations.cpp:2940-3006). */
 int nsg_imfill_holes_u8(nsg_context *ctx, const uint8_t *img, uint8_t *out, int rows, int cols, int conn,
                         nsg_stream_t stream);
+/* No counterpart in the reference.  The same hole filling as
+ * nsg_imfill_holes_u8 for callers that cannot allocate device memory and so
+ * cannot create an nsg_context (an embedding application that owns the device
+ * allocator, or code that must not allocate once it is set up).  It calls no
+ * cudaMalloc, cudaFree or allocating library routine; its work planes live in
+ * one static device array of NSG_NOALLOC_MAX_PIXELS * 8 bytes (32 MiB) that
+ * every GPU loading the library holds until the process exits.
+ *  - rows * cols above NSG_NOALLOC_MAX_PIXELS returns NSG_ERR_OOM; bad
+ *    pointers, sizes or connectivity return NSG_ERR_ARG.
+ *  - The first call on each device looks up the array's device address (with
+ *    that device current); make that first call before any stream capture.
+ *  - The call only enqueues work on `stream` and returns; `out` is ready when
+ *    the stream reaches it.  All calls share the one array, so calls whose
+ *    work overlaps on the GPU (other streams, other host threads) race:
+ *    order them on one stream or synchronise between them. */
+#define NSG_NOALLOC_MAX_PIXELS (4194304) /* e.g. 2048 x 2048 */
+int nsg_imfill_holes_u8_noalloc(const uint8_t *img, uint8_t *out, int rows, int cols, int conn,
+                                nsg_stream_t stream);
 /* nscale::bwselect<unsigned char>(bw, seeds, conn) (MorphologicOperations.cpp:3010-3031). */
 int nsg_bwselect_u8(nsg_context *ctx, const uint8_t *bw, const uint8_t *seeds, uint8_t *out, int rows, int cols,
                     int conn, nsg_stream_t stream);

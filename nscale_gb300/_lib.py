@@ -64,6 +64,7 @@ _SIGS = {
     "nsg_imreconstruct_f32": (_I, [_P, _P, _P, _P, _I, _I, _I, _P]),
     "nsg_imreconstruct_binary_u8": (_I, [_P, _P, _P, _P, _I, _I, _I, _P]),
     "nsg_imfill_holes_u8": (_I, [_P, _P, _P, _I, _I, _I, _P]),
+    "nsg_imfill_holes_u8_noalloc": (_I, [_P, _P, _I, _I, _I, _P]),
     "nsg_bwselect_u8": (_I, [_P, _P, _P, _P, _I, _I, _I, _P]),
     "nsg_bwlabel": (_I, [_P, _P, _P, _I, _I, _I, _P]),
     "nsg_bwareaopen": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, C.POINTER(_I), _P]),

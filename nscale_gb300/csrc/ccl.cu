@@ -23,6 +23,8 @@
 // touch a seed (or the image border), select".
 #include <limits.h>
 
+#include <mutex>
+
 #include "nsg_internal.cuh"
 
 namespace nsg {
@@ -590,4 +592,96 @@ int bbox_dev(Ctx &c, const int32_t *labels, int rows, int cols, int32_t *d_bbox,
     return NSG_SUCCESS;
 }
 
+// ---- imfillHoles with no allocation at all ----------------------------------
+// Some callers cannot create an nsg_context: code that runs where allocating
+// device memory is not allowed (a host that hands the library a memory budget
+// it has already spent, a plugin sandbox whose device allocator is owned by
+// the embedding application, or a process that must not allocate after its
+// set-up phase).  For them nsg_imfill_holes_u8_noalloc takes its two int32
+// work planes (component labels and per-component border flags) from one
+// file-scope device array instead of the context arena.  The array is part
+// of this library's device image: every GPU that loads the library holds it
+// (NSG_NOALLOC_MAX_PIXELS * 8 bytes) until the process exits.
+namespace {
+
+__device__ __align__(256) int g_noalloc_scratch[2 * (int64_t)NSG_NOALLOC_MAX_PIXELS];
+
+struct NoAllocScratch {
+    int *base = nullptr;  // device address of g_noalloc_scratch on this device
+    int sm_count = 0;
+};
+constexpr int kNoAllocDevices = 64;
+std::mutex g_noalloc_mu;
+NoAllocScratch g_noalloc[kNoAllocDevices];
+
+// Set-up, once per device and with that device current: the symbol name is
+// only a host-side handle, so the device address comes from the runtime.
+int noalloc_scratch(NoAllocScratch *out) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return NSG_ERR_CUDA;
+    }
+    if (dev < 0 || dev >= kNoAllocDevices) return NSG_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    NoAllocScratch &e = g_noalloc[dev];
+    if (!e.base) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+            cudaGetLastError();
+            return NSG_ERR_CUDA;
+        }
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+            cudaGetLastError();
+            return NSG_ERR_CUDA;
+        }
+        e.sm_count = sms;
+        e.base = static_cast<int *>(p);
+    }
+    *out = e;
+    return NSG_SUCCESS;
+}
+
+int noalloc_blocks(int sm_count, int64_t n) {
+    int64_t g = (n + kB - 1) / kB;
+    int64_t cap = (int64_t)sm_count * 16;
+    return (int)(g < 1 ? 1 : (g < cap ? g : cap));
+}
+
+}  // namespace
+
 }  // namespace nsg
+
+extern "C" int nsg_imfill_holes_u8_noalloc(const uint8_t *img, uint8_t *out, int rows, int cols, int conn,
+                                           nsg_stream_t stream) {
+    using namespace nsg;
+    if (!img || !out || rows <= 0 || cols <= 0 || (conn != 4 && conn != 8)) return NSG_ERR_ARG;
+    const int64_t n = (int64_t)rows * cols;
+    if (n > (int64_t)NSG_NOALLOC_MAX_PIXELS) return NSG_ERR_OOM;
+    NoAllocScratch sc;
+    int st = noalloc_scratch(&sc);
+    if (st != NSG_SUCCESS) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // Every call overwrites the labels of all rows*cols pixels and clears the
+    // flag of every component root before setting any, so nothing the
+    // previous call left in the array is read.
+    int *lab = sc.base, *flag = sc.base + (int64_t)NSG_NOALLOC_MAX_PIXELS;
+    PredU8 pr{img, CCL_NOT255};
+    const int g = noalloc_blocks(sc.sm_count, n);
+    dim3 grid((cols + LT - 1) / LT, (rows + LT - 1) / LT);
+    ccl_local<PredU8><<<grid, 256, 0, s>>>(pr, lab, rows, cols, conn);
+    NSG_COUNT_LAUNCH();
+    ccl_border<PredU8><<<g, kB, 0, s>>>(pr, lab, rows, cols, conn);
+    NSG_COUNT_LAUNCH();
+    ccl_flatten<<<g, kB, 0, s>>>(lab, n);
+    NSG_COUNT_LAUNCH();
+    zero_flags_at_roots<<<g, kB, 0, s>>>(lab, flag, n);
+    NSG_COUNT_LAUNCH();
+    flag_border<<<noalloc_blocks(sc.sm_count, 2 * (int64_t)rows + 2 * cols), kB, 0, s>>>(lab, flag, rows, cols);
+    NSG_COUNT_LAUNCH();
+    select_fill<<<g, kB, 0, s>>>(lab, flag, out, n);
+    NSG_COUNT_LAUNCH();
+    if (cudaGetLastError() != cudaSuccess) return NSG_ERR_CUDA;
+    return NSG_SUCCESS;
+}
