@@ -47,8 +47,8 @@ typedef struct nsg_context nsg_context;
 typedef void *nsg_stream_t; /* cudaStream_t */
 
 /* Parameters of segmentNuclei, same order, meaning and defaults as
- * HistologicalEntities.h:52-54 (logger / intermediate-result handler are
- * replaced by nsg_context_set_dump). */
+ * HistologicalEntities.h:52-54 (the logger is replaced by the per-stage
+ * timers, nsg_context_set_timing; there is no intermediate-result handler). */
 typedef struct nsg_seg_params {
     int blue, green, red;       /* 220 220 220 */
     double T1, T2;              /* 5.0 4.0 */
@@ -172,7 +172,9 @@ int nsg_watershed_serial(nsg_context *ctx, const uint8_t *bgr, const float *img,
 /* Diagnostics of the last nsg_watershed / segmentNuclei flood (16 ints):
  * [0] fallback code (0 = domain-parallel path taken), [1] flood domains,
  * [2] background entries recorded, [6] level of the first background pop,
- * [9] 1 if a background flood event happened, [11] BFS layers. */
+ * [9] 1 if a background flood event happened, [11] BFS layers; and of the
+ * last grey reconstruction: [12] tile passes, [13] row+column sweeps;
+ * [14] CTAs in the BFS cluster. */
 int nsg_watershed_diagnostics(nsg_context *ctx, int *out16, nsg_stream_t stream);
 /* ConnComponents::boundingBox (ConnComponents.cpp:241-284) on a -1-background
  * label image: writes compcount entries of (label, minx, maxx, miny, maxy) as

@@ -98,6 +98,8 @@ __global__ void init_queue(int *state, int *queue, int qcap, int ntiles, int *ct
         ctrl[C_QHEAD] = 0;
         ctrl[C_QTAIL] = ntiles;
         ctrl[C_QPEND] = ntiles;
+        ctrl[C_RSTATS] = 0;
+        ctrl[C_RSTATS + 1] = 0;
     }
 }
 
@@ -106,6 +108,7 @@ struct Queue {
     int *queue;
     int qcap;
     int *head, *tail, *outstanding, *status;
+    int *stats;  // [0] tile passes, [1] row+column sweeps (recon_cta)
     long long budget;
 };
 
@@ -384,10 +387,13 @@ struct TileSmem {
     static constexpr int OW = P;  // row pitch of the halo tile (elements)
     T o[(TH + 2) * P];
     T m[TH * TW];
+    T eN[TW], eS[TW], eW[TH], eE[TH];          // the tile's edge values when it was loaded
+    T mN[TW + 2], mS[TW + 2], mW[TH], mE[TH];  // the mask just outside the tile (neighbours' pixels)
     int edges;
     int changed;
     int tile;
     int again;
+    int sweeps;
 };
 
 // One line (row or column) of N = 32 * K pixels: forward then backward
@@ -471,9 +477,32 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
         int y = y0 + r, x = x0 + cc;
         sm.m[i] = (y < rows && x < cols) ? __ldg(mask + (int64_t)y * cols + x) : (T)0;
     }
-    if (threadIdx.x == 0) sm.edges = 0;
+    if (threadIdx.x == 0) {
+        sm.edges = 0;
+        sm.sweeps = 0;
+    }
+    auto mask_at = [&](int y, int x) -> T {
+        return (y >= 0 && y < rows && x >= 0 && x < cols) ? __ldg(mask + (int64_t)y * cols + x) : (T)0;
+    };
+    for (int i = threadIdx.x; i < TW + 2; i += NW * 32) {
+        sm.mN[i] = mask_at(y0 - 1, x0 - 1 + i);
+        sm.mS[i] = mask_at(y0 + TH, x0 - 1 + i);
+    }
+    for (int i = threadIdx.x; i < TH; i += NW * 32) {
+        sm.mW[i] = mask_at(y0 + i, x0 - 1);
+        sm.mE[i] = mask_at(y0 + i, x0 + TW);
+    }
     __syncthreads();
+    for (int i = threadIdx.x; i < TW; i += NW * 32) {
+        sm.eN[i] = o[P + i + 1];
+        sm.eS[i] = o[TH * P + i + 1];
+    }
+    for (int i = threadIdx.x; i < TH; i += NW * 32) {
+        sm.eW[i] = o[(i + 1) * P + 1];
+        sm.eE[i] = o[(i + 1) * P + TW];
+    }
     unsigned my_edges = 0;
+    bool anych = false;
     const int vr = rows - y0, vc = cols - x0;  // valid extent of this tile
     for (int it = 0; it < 1024; ++it) {
         bool ch = false;
@@ -500,10 +529,6 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
                 if (!(res[k] == cur[k])) {
                     row[x] = res[k];
                     ch = true;
-                    if (r == 0) my_edges |= 1u;
-                    if (r == TH - 1) my_edges |= 2u;
-                    if (x == 0) my_edges |= 4u;
-                    if (x == TW - 1) my_edges |= 8u;
                 }
             }
         }
@@ -530,23 +555,76 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
                 if (!(res[k] == cur[k])) {
                     o[(y + 1) * P + cidx + 1] = res[k];
                     ch = true;
-                    if (y == 0) my_edges |= 1u;
-                    if (y == TH - 1) my_edges |= 2u;
-                    if (cidx == 0) my_edges |= 4u;
-                    if (cidx == TW - 1) my_edges |= 8u;
                 }
             }
         }
-        if (!__syncthreads_or(ch)) break;
+        const bool any = __syncthreads_or(ch);
+        if (threadIdx.x == 0) sm.sweeps = it + 1;
+        if (!any) break;
+        anych = true;
         if (it == 1023) my_edges |= 16u;  // not stable yet: process again later
     }
-    if (my_edges) atomicOr(&sm.edges, (int)my_edges);
-    // write back
-    for (int i = threadIdx.x; i < TH * TW; i += NW * 32) {
-        int r = i / TW, cc = i - r * TW;
-        int y = y0 + r, x = x0 + cc;
-        if (y < rows && x < cols) out[(int64_t)y * cols + x] = o[(r + 1) * P + cc + 1];
+    // A neighbour tile needs another pass only if an edge pixel that changed
+    // here can raise one of its pixels: new value above that pixel's value
+    // (as loaded; it can only have grown since) and that pixel below its mask.
+    if (anych) {
+        const int c8 = conn8 ? 1 : 0;
+        for (int x = threadIdx.x; x < TW; x += NW * 32) {
+            T v = o[P + x + 1];
+            if (!(v == sm.eN[x]))
+                for (int d = -c8; d <= c8; ++d) {
+                    int h = x + d;
+                    if (h < 0 || h >= TW) continue;
+                    T hv = o[h + 1];
+                    if (v > hv && sm.mN[h + 1] > hv) my_edges |= 1u;
+                }
+            v = o[TH * P + x + 1];
+            if (!(v == sm.eS[x]))
+                for (int d = -c8; d <= c8; ++d) {
+                    int h = x + d;
+                    if (h < 0 || h >= TW) continue;
+                    T hv = o[(TH + 1) * P + h + 1];
+                    if (v > hv && sm.mS[h + 1] > hv) my_edges |= 2u;
+                }
+        }
+        for (int y = threadIdx.x; y < TH; y += NW * 32) {
+            T v = o[(y + 1) * P + 1];
+            if (!(v == sm.eW[y]))
+                for (int d = -c8; d <= c8; ++d) {
+                    int h = y + d;
+                    if (h < 0 || h >= TH) continue;
+                    T hv = o[(h + 1) * P];
+                    if (v > hv && sm.mW[h] > hv) my_edges |= 4u;
+                }
+            v = o[(y + 1) * P + TW];
+            if (!(v == sm.eE[y]))
+                for (int d = -c8; d <= c8; ++d) {
+                    int h = y + d;
+                    if (h < 0 || h >= TH) continue;
+                    T hv = o[(h + 1) * P + TW + 1];
+                    if (v > hv && sm.mE[h] > hv) my_edges |= 8u;
+                }
+        }
+        if (c8 && threadIdx.x == 0) {
+            T v, hv;
+            v = o[P + 1], hv = o[0];
+            if (!(v == sm.eN[0]) && v > hv && sm.mN[0] > hv) my_edges |= 32u;  // up-left
+            v = o[P + TW], hv = o[TW + 1];
+            if (!(v == sm.eN[TW - 1]) && v > hv && sm.mN[TW + 1] > hv) my_edges |= 64u;  // up-right
+            v = o[TH * P + 1], hv = o[(TH + 1) * P];
+            if (!(v == sm.eS[0]) && v > hv && sm.mS[0] > hv) my_edges |= 128u;  // down-left
+            v = o[TH * P + TW], hv = o[(TH + 1) * P + TW + 1];
+            if (!(v == sm.eS[TW - 1]) && v > hv && sm.mS[TW + 1] > hv) my_edges |= 256u;  // down-right
+        }
     }
+    if (my_edges) atomicOr(&sm.edges, (int)my_edges);
+    // write back (only a tile that changed)
+    if (anych)
+        for (int i = threadIdx.x; i < TH * TW; i += NW * 32) {
+            int r = i / TW, cc = i - r * TW;
+            int y = y0 + r, x = x0 + cc;
+            if (y < rows && x < cols) out[(int64_t)y * cols + x] = o[(r + 1) * P + cc + 1];
+        }
     __threadfence();
     __syncthreads();
 }
@@ -574,12 +652,12 @@ __global__ void __launch_bounds__(256) recon_cta(const T *__restrict__ mask, T *
                 if (edges & 2u && ty + 1 < tiles_y) q_push(q, t + tiles_x);
                 if (edges & 4u && tx > 0) q_push(q, t - 1);
                 if (edges & 8u && tx + 1 < tiles_x) q_push(q, t + 1);
-                if (conn8) {
-                    if ((edges & 5u) == 5u && ty > 0 && tx > 0) q_push(q, t - tiles_x - 1);
-                    if ((edges & 9u) == 9u && ty > 0 && tx + 1 < tiles_x) q_push(q, t - tiles_x + 1);
-                    if ((edges & 6u) == 6u && ty + 1 < tiles_y && tx > 0) q_push(q, t + tiles_x - 1);
-                    if ((edges & 10u) == 10u && ty + 1 < tiles_y && tx + 1 < tiles_x) q_push(q, t + tiles_x + 1);
-                }
+                if (edges & 32u && ty > 0 && tx > 0) q_push(q, t - tiles_x - 1);
+                if (edges & 64u && ty > 0 && tx + 1 < tiles_x) q_push(q, t - tiles_x + 1);
+                if (edges & 128u && ty + 1 < tiles_y && tx > 0) q_push(q, t + tiles_x - 1);
+                if (edges & 256u && ty + 1 < tiles_y && tx + 1 < tiles_x) q_push(q, t + tiles_x + 1);
+                atomicAdd(q.stats, 1);
+                atomicAdd(q.stats + 1, sm.sweeps);
                 sm.again = q_finish(q, t);
             }
             __syncthreads();
@@ -625,6 +703,7 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
     q.outstanding = c.ws.ctrl + C_QPEND;
     q.status = c.ws.ctrl + C_STATUS;
     q.budget = c.spin_budget;
+    q.stats = c.ws.ctrl + C_RSTATS;
     const size_t smem = sizeof(TileSmem<T, TW, TH, P>);
     auto kfn = recon_cta<T, TW, TH, P>;
     NSG_CUDA_TRY(c, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -673,6 +752,7 @@ int run_recon(Ctx &c, const T *marker, const T *mask, T *out, int rows, int cols
     q.outstanding = c.ws.ctrl + C_QPEND;
     q.status = c.ws.ctrl + C_STATUS;
     q.budget = c.spin_budget;
+    q.stats = c.ws.ctrl + C_RSTATS;
     const size_t smem = (size_t)WARPS * ((TH + 2) * (TW + 2) + TH * TW) * sizeof(T);
     auto kfn = recon_persistent<T, TH, WARPS>;
     NSG_CUDA_TRY(c, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

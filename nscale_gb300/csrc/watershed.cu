@@ -104,9 +104,12 @@ int watershed_serial_dev(Ctx &c, const uint8_t *bgr, const float *img, int32_t *
 // block): [0] fallback code (0 = domain-parallel path), [1] domains,
 // [2] dummy entries, [6] level of the first background pop, [11] BFS layers.
 int watershed_diag(Ctx &c, int *out16, cudaStream_t s) {
-    NSG_CUDA_TRY(c, cudaMemcpyAsync(c.ws.h_ctrl, c.ws.ctrl + C_WS, 16 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    NSG_CUDA_TRY(c, cudaMemcpyAsync(c.ws.h_ctrl, c.ws.ctrl + C_WS, 13 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    NSG_CUDA_TRY(c, cudaMemcpyAsync(c.ws.h_ctrl + 14, c.ws.ctrl + C_WS + 12, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NSG_CUDA_TRY(c, cudaMemcpyAsync(c.ws.h_ctrl + 12, c.ws.ctrl + C_RSTATS, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
     NSG_CUDA_TRY(c, cudaStreamSynchronize(s));
-    for (int i = 0; i < 16; ++i) out16[i] = c.ws.h_ctrl[i];
+    for (int i = 0; i < 15; ++i) out16[i] = c.ws.h_ctrl[i];
+    out16[15] = 0;
     return NSG_SUCCESS;
 }
 

@@ -42,6 +42,8 @@
 // device flag makes the serial flood (ws_flood_serial) produce the result.
 #include <limits.h>
 
+#include <cooperative_groups.h>
+
 #include "nsg_internal.cuh"
 
 namespace nsg {
@@ -75,6 +77,7 @@ enum {
     W_EVENT,
     W_PEND,
     W_LAYERS,
+    W_BFSCTAS,
 };
 
 struct PW {
@@ -529,69 +532,148 @@ __device__ int cta_exclusive_scan(int v, int *sh, int &total) {
     return r;
 }
 
-// FIFO BFS from e over black unknown pixels that are not queued at T_e: the
-// pop rank of each R pixel is its position in the frontier sequence; every
-// state-0 fg neighbour records the smallest (rank * 4 + direction) that
-// touches it, which is the order in which R pushes it.
-__global__ void __launch_bounds__(1024) k_bfs(PW a) {
-    __shared__ int sh[40];
-    if (!a.ctl[W_EVENT] || a.ctl[W_FALLBACK]) return;
-    const int W = a.W;
-    int *F0 = a.fr0, *F1 = a.fr1;
-    int s = 1, base = 0, layers = 0;
-    if (threadIdx.x == 0) F0[0] = a.ctl[W_EP];
-    __syncthreads();
-    const int off[4] = {-1, 1, -W, W};
-    while (s > 0) {
-        const int per = (s + blockDim.x - 1) / blockDim.x;
-        const int i0 = threadIdx.x * per, i1 = min(s, i0 + per);
-        for (int i = i0; i < i1; ++i) {
-            int r = __ldcg(F0 + i);
+// Neighbour classes of every pixel R can contain (a black unknown pixel not
+// queued at T_e, e included): bit k (k = left, right, up, down) when the
+// neighbour in direction k is a black unknown pixel R may still enter, bit
+// 4 + k when it is an fg pixel R would push (neither popped nor queued at
+// T_e).  Both are fixed during the BFS, so a frontier pixel costs one byte.
+__global__ void k_bfs_prep(PW a, uint8_t *nbm) {
+    const bool on = a.ctl[W_EVENT] && !a.ctl[W_FALLBACK];
+    const int off[4] = {-1, 1, -a.W, a.W};
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
+        const uint8_t f = a.flags[p];
+        uint8_t m = 0;
+        if (on && (f & F_U) && !(f & F_BORDER) && !(a.st[p] & S_QUEUED)) {
+#pragma unroll
             for (int k = 0; k < 4; ++k) {
-                int qq = r + off[k];
-                uint8_t f = a.flags[qq];
-                if (!(f & F_UNK)) continue;
-                uint8_t sq = __ldcg(a.st + qq);
-                if (f & F_U) {
-                    if (sq & (S_QUEUED | S_R)) continue;
-                    atomicMin(a.claim + qq, i * 4 + k);
+                const int q = p + off[k];
+                const uint8_t fq = a.flags[q], sq = a.st[q];
+                if (!(fq & F_UNK)) continue;
+                if (fq & F_U) {
+                    if (!(sq & (S_QUEUED | S_R))) m |= (uint8_t)(1u << k);
                 } else if (!(sq & (S_POPPED | S_QUEUED))) {
-                    atomicMin(a.inj + qq, (base + i) * 4 + k);
+                    m |= (uint8_t)(16u << k);
                 }
             }
         }
-        __syncthreads();
-        int cnt = 0;
-        for (int i = i0; i < i1; ++i) {
-            int r = __ldcg(F0 + i);
-            for (int k = 0; k < 4; ++k) {
-                int qq = r + off[k];
-                if ((a.flags[qq] & F_U) && __ldcg(a.claim + qq) == i * 4 + k) ++cnt;
+        nbm[p] = m;
+    }
+}
+
+// FIFO BFS from e over black unknown pixels that are not queued at T_e.  The
+// pop rank of an R pixel is its position in the frontier sequence; a pixel
+// joins the next frontier through the earliest frontier pixel that touches
+// it, in the order (frontier position, direction).  Claims use the key
+// rank * 4 + direction with atomicMin: keys grow from layer to layer, so a
+// pixel claimed in an earlier layer keeps its key and is never taken again,
+// and the smallest key of a layer is its FIFO owner.  Every fg neighbour that
+// is neither popped nor queued at T_e records the smallest key that touches
+// it: the order in which R pushes it.
+//
+// One thread-block cluster runs the BFS (one CTA per SM, up to 16).  A layer
+// is split into contiguous chunks, one per CTA; after the claims a cluster
+// barrier, then each CTA compacts its winners in order into its own segment
+// of the next frontier and publishes their count in shared memory; after a
+// second barrier every CTA reads all counts (distributed shared memory) to
+// place the segments.  Chunks are contiguous and ordered by CTA, so the next
+// frontier in global order is the concatenation of the segments.
+constexpr int kBfsThreads = 1024, kBfsItems = 8, kBfsMaxCluster = 16;
+
+__global__ void __launch_bounds__(kBfsThreads, 1) k_bfs(PW a, const uint8_t *__restrict__ nbm) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const int C = (int)cl.num_blocks(), me = (int)cl.block_rank();
+    __shared__ int sh[40];
+    __shared__ int tot;                      // winners of this CTA in the last layer
+    __shared__ int offs[kBfsMaxCluster + 1];  // where each CTA's segment starts in global order
+    const bool on = a.ctl[W_EVENT] && !a.ctl[W_FALLBACK];
+    const int W = a.W;
+    int *Fc = a.fr0, *Fn = a.fr1;
+    if (threadIdx.x == 0) {
+        tot = me == 0 ? 1 : 0;
+        if (me == 0 && on) Fc[0] = a.ctl[W_EP];
+    }
+    cl.sync();  // every CTA has read the control flags before anything can change them
+    if (!on) return;
+    const int off[4] = {-1, 1, -W, W};
+    int prevcap = 1, base = 0, layer = 0;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            int acc = 0;
+            for (int j = 0; j < C; ++j) {
+                offs[j] = acc;
+                acc += *cl.map_shared_rank(&tot, j);
             }
+            offs[C] = acc;
+        }
+        __syncthreads();
+        const int s = offs[C];
+        if (s == 0) break;
+        const int per_cta = (s + C - 1) / C;
+        const int segcap = 4 * per_cta;
+        if (per_cta > kBfsThreads * kBfsItems || (int64_t)segcap * C > (int64_t)a.n) {
+            if (me == 0 && threadIdx.x == 0) set_fallback(a, 9);  // frontier too wide: serial flood
+            break;
+        }
+        const int lo = min(s, me * per_cta), hi = min(s, lo + per_cta);
+        const int pt = (hi - lo + kBfsThreads - 1) / kBfsThreads;
+        const int i0 = lo + threadIdx.x * pt;
+        int rr[kBfsItems];
+        uint8_t mm[kBfsItems];
+        int seg = 0;
+#pragma unroll
+        for (int j = 0; j < kBfsItems; ++j) {
+            const int i = i0 + j;
+            rr[j] = -1;
+            mm[j] = 0;
+            if (j < pt && i < hi) {
+                while (i >= offs[seg + 1]) ++seg;
+                rr[j] = __ldcg(Fc + seg * prevcap + (i - offs[seg]));
+                mm[j] = nbm[rr[j]];
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kBfsItems; ++j) {
+            const int key0 = (base + i0 + j) * 4;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (mm[j] & (1u << k)) atomicMin(a.claim + rr[j] + off[k], key0 + k);
+                if (mm[j] & (16u << k)) atomicMin(a.inj + rr[j] + off[k], key0 + k);
+            }
+        }
+        cl.sync();
+        unsigned win = 0;
+#pragma unroll
+        for (int j = 0; j < kBfsItems; ++j) {
+            const int key0 = (base + i0 + j) * 4;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if ((mm[j] & (1u << k)) && __ldcg(a.claim + rr[j] + off[k]) == key0 + k) win |= 1u << (j * 4 + k);
         }
         int total;
-        int pos = cta_exclusive_scan(cnt, sh, total);
-        for (int i = i0; i < i1; ++i) {
-            int r = __ldcg(F0 + i);
-            for (int k = 0; k < 4; ++k) {
-                int qq = r + off[k];
-                if ((a.flags[qq] & F_U) && __ldcg(a.claim + qq) == i * 4 + k) {
-                    F1[pos++] = qq;
-                    a.st[qq] |= S_R;
-                    a.claim[qq] = INT_MAX;
-                }
-            }
+        int pos = cta_exclusive_scan(__popc(win), sh, total);
+        while (win) {
+            const int b = __ffs(win) - 1;
+            win &= win - 1;
+            const int q = rr[b >> 2] + off[b & 3];
+            Fn[me * segcap + pos] = q;
+            a.st[q] |= S_R;
+            ++pos;
         }
-        __threadfence_block();
-        __syncthreads();
-        int *t = F0;
-        F0 = F1;
-        F1 = t;
+        if (threadIdx.x == 0) tot = total;
+        int *t = Fc;
+        Fc = Fn;
+        Fn = t;
+        prevcap = segcap;
         base += s;
-        s = total;
-        ++layers;
+        ++layer;
+        cl.sync();
     }
-    if (threadIdx.x == 0) a.ctl[W_LAYERS] = layers;
+    cl.sync();  // no CTA leaves while another may still read its shared counts
+    if (me == 0 && threadIdx.x == 0) {
+        a.ctl[W_LAYERS] = layer;
+        a.ctl[W_BFSCTAS] = C;
+    }
 }
 
 // shells: U pixels queued at T_e
@@ -1200,6 +1282,36 @@ int ws_flood_serial_launch(Ctx &c, const int *mk, const uint32_t *col, int *outp
     return NSG_SUCCESS;
 }
 
+// The BFS cluster: 16 CTAs when the device can co-schedule them, else fewer.
+static int launch_bfs(Ctx &c, const PW &a, const uint8_t *nbm, cudaStream_t s) {
+    NSG_CUDA_TRY(c, cudaFuncSetAttribute(k_bfs, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    cfg.blockDim = dim3(kBfsThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int cl = kBfsMaxCluster;
+    for (; cl > 1; cl /= 2) {
+        cfg.gridDim = dim3(cl);
+        attr[0].val.clusterDim.x = cl;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, k_bfs, &cfg) == cudaSuccess && nclusters >= 1) break;
+        cudaGetLastError();
+    }
+    cfg.gridDim = dim3(cl);
+    attr[0].val.clusterDim.x = cl;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    NSG_CUDA_TRY(c, cudaLaunchKernelEx(&cfg, k_bfs, a, nbm));
+    NSG_COUNT_LAUNCH();
+    return NSG_SUCCESS;
+}
+
 int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int W, cudaStream_t s) {
     PW a;
     a.H = H;
@@ -1250,8 +1362,9 @@ int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int 
     NSG_COUNT_LAUNCH();
     k_event_label<<<1, 32, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
-    k_bfs<<<1, 1024, 0, s>>>(a);
+    k_bfs_prep<<<g, kB, 0, s>>>(a, a.fgimg);  // the domain image is no longer needed
     NSG_COUNT_LAUNCH();
+    NSG_TRY(launch_bfs(c, a, a.fgimg, s));
     NSG_LAUNCH_CHECK(c);
     k_shells<<<g, kB, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
