@@ -5,23 +5,26 @@
 // scan, then a FIFO wavefront.  Its result is the unique least fixed point
 //     out = max(min(marker, mask), min(max over conn-neighbours of out, mask))
 // on the image padded with a one-pixel ring of value 0 (marker and mask),
-// so any propagation order reproduces it exactly; that is what this kernel
-// does, GB300-style:
+// so any propagation order reproduces it exactly; this file computes it with
+// one persistent kernel:
 //
-//  * the image is cut into 64-wide tiles; ONE WARP owns a tile at a time and
-//    keeps it (plus a one-pixel halo) in shared memory;
-//  * inside the tile the warp runs the reference's raster / anti-raster
-//    scans row by row: the vertical step is elementwise, the horizontal
-//    dependence  out[x] = min(max(v[x], out[x-1]), mask[x])  is a prefix
-//    composition of clamp functions, evaluated with warp shuffles (a scan of
-//    (lo, hi) pairs), so a whole row propagates in log2(32) steps;
-//  * scans repeat until the tile is stable; changed tile edges re-queue the
-//    neighbouring tiles;
-//  * tiles circulate through a device-resident work queue inside ONE
-//    persistent kernel (the queue wavefront): no host round trip until the
-//    whole image has converged.  A per-tile state machine (idle / queued /
-//    processing / processing+requeue) guarantees one warp per tile, and one
-//    `outstanding` counter detects global termination.  Every wait is
+//  * the image is cut into tiles (128 x 128 uint8, 64 x 64 float32); a CTA
+//    owns a tile at a time and keeps it, a one-pixel halo and its mask in
+//    shared memory;
+//  * inside the tile, row phases and column phases alternate.  In a row
+//    phase each warp takes whole rows: the cross-row step (the neighbours in
+//    the rows above and below) is elementwise, and the along-row dependence
+//    out[x] = clamp(out[x-1], lo[x], hi[x]) of the raster and anti-raster
+//    scans is a composition of clamp functions, evaluated as a prefix scan
+//    with warp shuffles; column phases do the same down and up the columns;
+//  * only dirty lines are scanned: a pixel changed by a row phase dirties its
+//    column and the two next to it for the following column phase, and the
+//    other way round, so a pass costs what actually propagates;
+//  * a tile whose edge changed in a way that can raise a neighbour's pixel
+//    queues that neighbour with the neighbour's edge line marked dirty;
+//    tiles circulate through a device-resident work queue (idle / queued /
+//    processing / processing+requeue per tile) and an `outstanding` counter
+//    detects global termination, with no host round trip.  Every wait is
 //    bounded by the context's spin budget and reports NSG_ERR_TIMEOUT.
 #include <float.h>
 #include <math.h>
@@ -31,8 +34,6 @@
 namespace nsg {
 
 namespace {
-
-constexpr int TW = 64;  // tile width (2 pixels per lane)
 
 // std::max / std::min as the reference writes them
 template <typename T>
@@ -89,10 +90,16 @@ __global__ void init_min_f32(const float *__restrict__ a, const float *__restric
     }
 }
 
-__global__ void init_queue(int *state, int *queue, int qcap, int ntiles, int *ctrl) {
+// dirty lines a tile starts a pass with (set by the tiles that notify it)
+enum : int { D_N = 1, D_S = 2, D_W = 4, D_E = 8, D_ALL = 16 };
+
+__global__ void init_queue(int *state, int *queue, int *dirty, int qcap, int ntiles, int *ctrl) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < qcap; i += gridDim.x * blockDim.x) {
         queue[i] = i < ntiles ? i + 1 : 0;
-        if (i < ntiles) state[i] = 1;
+        if (i < ntiles) {
+            state[i] = 1;
+            dirty[i] = D_ALL;
+        }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         ctrl[C_QHEAD] = 0;
@@ -108,7 +115,8 @@ struct Queue {
     int *queue;
     int qcap;
     int *head, *tail, *outstanding, *status;
-    int *stats;  // [0] tile passes, [1] row+column sweeps (recon_cta)
+    int *dirty;  // per tile: D_* bits for its next pass
+    int *stats;  // [0] tile passes, [1] row+column sweeps
     long long budget;
 };
 
@@ -182,219 +190,37 @@ __device__ int q_finish(Queue &q, int t) {
     return 1;
 }
 
-template <typename T, int TH>
-__device__ void process_tile(const T *__restrict__ mask, T *out, int rows, int cols, bool conn8, int tx, int ty,
-                             T *o, T *m, unsigned &edges) {
-    const int lane = threadIdx.x & 31;
-    const int OW = TW + 2;
-    const int y0 = ty * TH, x0 = tx * TW;
-    // load tile + halo (ring outside the image = 0)
-    for (int i = lane; i < (TH + 2) * OW; i += 32) {
-        int r = i / OW, cc = i - r * OW;
-        int y = y0 - 1 + r, x = x0 - 1 + cc;
-        o[i] = (y >= 0 && y < rows && x >= 0 && x < cols) ? ldcg(out + (int64_t)y * cols + x) : (T)0;
-    }
-    for (int i = lane; i < TH * TW; i += 32) {
-        int r = i / TW, cc = i - r * TW;
-        int y = y0 + r, x = x0 + cc;
-        m[i] = (y < rows && x < cols) ? __ldg(mask + (int64_t)y * cols + x) : (T)0;
-    }
-    __syncwarp();
-    const int xa = 2 * lane, xb = 2 * lane + 1;
-    const bool ina = (x0 + xa) < cols, inb = (x0 + xb) < cols;
-    unsigned my_edges = 0;
-    bool any = true;
-    for (int it = 0; any && it < 4096; ++it) {
-        any = false;
-        // forward (raster) scan
-        for (int r = 0; r < TH; ++r) {
-            const bool rowin = (y0 + r) < rows;
-            T *orow = o + (r + 1) * OW + 1;
-            const T *up = orow - OW;
-            T ca = orow[xa], cb = orow[xb];
-            T wa = smax(ca, up[xa]), wb = smax(cb, up[xb]);
-            if (conn8) {
-                wa = smax(wa, smax(up[xa - 1], up[xa + 1]));
-                wb = smax(wb, smax(up[xb - 1], up[xb + 1]));
-            }
-            T ma = m[r * TW + xa], mb = m[r * TW + xb];
-            T loa, hia, lob, hib;
-            if (rowin && ina) { loa = smin(wa, ma); hia = ma; } else { loa = (T)0; hia = (T)0; }
-            if (rowin && inb) { lob = smin(wb, mb); hib = mb; } else { lob = (T)0; hib = (T)0; }
-            // lane function F = f_b o f_a
-            T lo = clampv(loa, lob, hib), hi = clampv(hia, lob, hib);
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                T pl = shfl_up(lo, d), ph = shfl_up(hi, d);
-                if (lane >= d) {
-                    T nl = clampv(pl, lo, hi), nh = clampv(ph, lo, hi);
-                    lo = nl;
-                    hi = nh;
-                }
-            }
-            T el = shfl_up(lo, 1), eh = shfl_up(hi, 1);
-            T left = orow[-1];
-            T in = lane == 0 ? left : clampv(left, el, eh);
-            T na = clampv(in, loa, hia);
-            T nb = clampv(na, lob, hib);
-            if (rowin && ina && !(na == ca)) {
-                orow[xa] = na;
-                any = true;
-                if (r == 0) my_edges |= 1u;
-                if (r == TH - 1) my_edges |= 2u;
-                if (xa == 0) my_edges |= 4u;
-            }
-            if (rowin && inb && !(nb == cb)) {
-                orow[xb] = nb;
-                any = true;
-                if (r == 0) my_edges |= 1u;
-                if (r == TH - 1) my_edges |= 2u;
-                if (xb == TW - 1) my_edges |= 8u;
-            }
-            __syncwarp();
-        }
-        // backward (anti-raster) scan
-        for (int r = TH - 1; r >= 0; --r) {
-            const bool rowin = (y0 + r) < rows;
-            T *orow = o + (r + 1) * OW + 1;
-            const T *dn = orow + OW;
-            T ca = orow[xa], cb = orow[xb];
-            T wa = smax(ca, dn[xa]), wb = smax(cb, dn[xb]);
-            if (conn8) {
-                wa = smax(wa, smax(dn[xa - 1], dn[xa + 1]));
-                wb = smax(wb, smax(dn[xb - 1], dn[xb + 1]));
-            }
-            T ma = m[r * TW + xa], mb = m[r * TW + xb];
-            T loa, hia, lob, hib;
-            if (rowin && ina) { loa = smin(wa, ma); hia = ma; } else { loa = (T)0; hia = (T)0; }
-            if (rowin && inb) { lob = smin(wb, mb); hib = mb; } else { lob = (T)0; hib = (T)0; }
-            // right-to-left: lane function F = f_a o f_b
-            T lo = clampv(lob, loa, hia), hi = clampv(hib, loa, hia);
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                T pl = shfl_down(lo, d), ph = shfl_down(hi, d);
-                if (lane + d < 32) {
-                    T nl = clampv(pl, lo, hi), nh = clampv(ph, lo, hi);
-                    lo = nl;
-                    hi = nh;
-                }
-            }
-            T el = shfl_down(lo, 1), eh = shfl_down(hi, 1);
-            T right = orow[TW];
-            T in = lane == 31 ? right : clampv(right, el, eh);
-            T nb = clampv(in, lob, hib);
-            T na = clampv(nb, loa, hia);
-            if (rowin && inb && !(nb == cb)) {
-                orow[xb] = nb;
-                any = true;
-                if (r == 0) my_edges |= 1u;
-                if (r == TH - 1) my_edges |= 2u;
-                if (xb == TW - 1) my_edges |= 8u;
-            }
-            if (rowin && ina && !(na == ca)) {
-                orow[xa] = na;
-                any = true;
-                if (r == 0) my_edges |= 1u;
-                if (r == TH - 1) my_edges |= 2u;
-                if (xa == 0) my_edges |= 4u;
-            }
-            __syncwarp();
-        }
-        any = __any_sync(0xffffffffu, any);
-    }
-    // edge changes (bits 0-3) and "not yet stable" (bit 4: re-queue self)
-    if (any) my_edges |= 16u;
-    edges = __reduce_or_sync(0xffffffffu, my_edges);
-    // write back
-    for (int i = lane; i < TH * TW; i += 32) {
-        int r = i / TW, cc = i - r * TW;
-        int y = y0 + r, x = x0 + cc;
-        if (y < rows && x < cols) out[(int64_t)y * cols + x] = o[(r + 1) * OW + cc + 1];
-    }
-    __threadfence();
-    __syncwarp();
-}
-
-template <typename T, int TH, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) recon_persistent(const T *__restrict__ mask, T *out, int rows, int cols,
-                                                              int conn, int tiles_x, int tiles_y, Queue q) {
-    extern __shared__ __align__(16) unsigned char sm_raw[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int per_warp = (TH + 2) * (TW + 2) + TH * TW;
-    T *o = reinterpret_cast<T *>(sm_raw) + warp * per_warp;
-    T *m = o + (TH + 2) * (TW + 2);
-    const bool conn8 = conn == 8;
-    for (;;) {
-        int t = 0;
-        if (lane == 0) t = q_pop(q);
-        t = __shfl_sync(0xffffffffu, t, 0);
-        if (t < 0) break;
-        __threadfence();
-        int again;
-        do {
-            int tx = t % tiles_x, ty = t / tiles_x;
-            unsigned edges = 0;
-            process_tile<T, TH>(mask, out, rows, cols, conn8, tx, ty, o, m, edges);
-            if (lane == 0 && edges) {
-                // corner pixels changed?  (tracked through the edge bits: a
-                // change on two perpendicular edges may involve a corner, so
-                // diagonal tiles are re-queued conservatively)
-                if (edges & 16u) q_push(q, t);
-                if (edges & 1u && ty > 0) q_push(q, t - tiles_x);
-                if (edges & 2u && ty + 1 < tiles_y) q_push(q, t + tiles_x);
-                if (edges & 4u && tx > 0) q_push(q, t - 1);
-                if (edges & 8u && tx + 1 < tiles_x) q_push(q, t + 1);
-                if (conn8) {
-                    if ((edges & 5u) == 5u && ty > 0 && tx > 0) q_push(q, t - tiles_x - 1);
-                    if ((edges & 9u) == 9u && ty > 0 && tx + 1 < tiles_x) q_push(q, t - tiles_x + 1);
-                    if ((edges & 6u) == 6u && ty + 1 < tiles_y && tx > 0) q_push(q, t + tiles_x - 1);
-                    if ((edges & 10u) == 10u && ty + 1 < tiles_y && tx + 1 < tiles_x) q_push(q, t + tiles_x + 1);
-                }
-            }
-            again = 0;
-            if (lane == 0) again = q_finish(q, t);
-            again = __shfl_sync(0xffffffffu, again, 0);
-            if (again) __threadfence();
-        } while (again);
-    }
-}
-
-// ---------------------------------------------------------------------------
-// CTA-per-tile variant: one CTA (8 warps) owns a TW x TH tile.  Row phases
-// scan every row of the tile in parallel (one warp per row at a time, PX
-// pixels per lane, clamp-function prefix scans left->right then right->left,
-// vertical and diagonal neighbours taken from the current tile); column
-// phases do the same down and up the columns.  Phases alternate until a
-// whole phase pair changes nothing: then every pixel satisfies the 8- (or 4-)
-// neighbour fixed-point equation inside the tile.  Concurrent reads of rows
-// other warps are updating are benign: values only grow and stay below the
-// fixed point.
-template <typename T>
-__device__ __forceinline__ T ident_lo();
-template <>
-__device__ __forceinline__ uint8_t ident_lo<uint8_t>() { return 0; }
-template <>
-__device__ __forceinline__ float ident_lo<float>() { return -INFINITY; }
-template <typename T>
-__device__ __forceinline__ T ident_hi();
-template <>
-__device__ __forceinline__ uint8_t ident_hi<uint8_t>() { return 255; }
-template <>
-__device__ __forceinline__ float ident_hi<float>() { return INFINITY; }
-
 template <typename T, int TW, int TH, int P>
 struct TileSmem {
-    static constexpr int OW = P;  // row pitch of the halo tile (elements)
-    T o[(TH + 2) * P];
-    T m[TH * TW];
+    T o[(TH + 2) * P];                         // the tile and its halo (row pitch P)
+    T m[TH * TW];                              // the mask
     T eN[TW], eS[TW], eW[TH], eE[TH];          // the tile's edge values when it was loaded
     T mN[TW + 2], mS[TW + 2], mW[TH], mE[TH];  // the mask just outside the tile (neighbours' pixels)
-    int edges;
-    int changed;
-    int tile;
-    int again;
-    int sweeps;
+    unsigned drow[TH / 32], dcol[TW / 32];     // dirty rows / columns
+    int edges, tile, again, sweeps, dirty;
 };
+
+// Whole warp: lane l changed the pixels of its K-pixel slice (l*K .. l*K+K-1)
+// given by the bits of `changed`; mark those lines and the lines next to
+// them in the N-line dirty set `m` (one shared-memory atomic per word).
+template <int K, int N>
+__device__ __forceinline__ void mark_dirty(unsigned *m, unsigned changed) {
+    constexpr int NWORD = N / 32;
+    const int lane = threadIdx.x & 31;
+    unsigned w[NWORD];
+#pragma unroll
+    for (int j = 0; j < NWORD; ++j) {
+        const unsigned mine = ((lane * K) >> 5) == j ? changed << ((lane * K) & 31) : 0u;
+        w[j] = __reduce_or_sync(0xffffffffu, mine);
+    }
+#pragma unroll
+    for (int j = 0; j < NWORD; ++j) {
+        unsigned d = w[j] | (w[j] << 1) | (w[j] >> 1);
+        if (j > 0) d |= w[j - 1] >> 31;
+        if (j + 1 < NWORD) d |= w[j + 1] << 31;
+        if (lane == j && d) atomicOr(&m[j], d);
+    }
+}
 
 // One line (row or column) of N = 32 * K pixels: forward then backward
 // clamp scans.  get(i) / put(i, v) address pixel i of the line (i = lane*K+k),
@@ -458,9 +284,12 @@ __device__ __forceinline__ void line_scan(T (&lo)[K], T (&hi)[K], T first, T las
     }
 }
 
+// One pass over tile (tx, ty): load, alternate row / column phases over the
+// dirty lines until nothing changes, report which neighbours must run again,
+// write back.
 template <typename T, int TW, int TH, int P>
 __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, int cols, bool conn8, int tx, int ty,
-                                 TileSmem<T, TW, TH, P> &sm) {
+                                 int dirty_in, TileSmem<T, TW, TH, P> &sm) {
     constexpr int NW = 8;
     constexpr int KX = TW / 32, KY = TH / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -477,10 +306,6 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
         int y = y0 + r, x = x0 + cc;
         sm.m[i] = (y < rows && x < cols) ? __ldg(mask + (int64_t)y * cols + x) : (T)0;
     }
-    if (threadIdx.x == 0) {
-        sm.edges = 0;
-        sm.sweeps = 0;
-    }
     auto mask_at = [&](int y, int x) -> T {
         return (y >= 0 && y < rows && x >= 0 && x < cols) ? __ldg(mask + (int64_t)y * cols + x) : (T)0;
     };
@@ -491,6 +316,25 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
     for (int i = threadIdx.x; i < TH; i += NW * 32) {
         sm.mW[i] = mask_at(y0 + i, x0 - 1);
         sm.mE[i] = mask_at(y0 + i, x0 + TW);
+    }
+    const bool all = dirty_in & D_ALL;
+    if (threadIdx.x < TH / 32) {
+        const int w = threadIdx.x;
+        unsigned b = all ? ~0u : 0u;
+        if ((dirty_in & D_N) && w == 0) b |= 1u;
+        if ((dirty_in & D_S) && w == TH / 32 - 1) b |= 1u << 31;
+        sm.drow[w] = b;
+    }
+    if (threadIdx.x >= 32 && threadIdx.x < 32 + TW / 32) {
+        const int w = threadIdx.x - 32;
+        unsigned b = all ? ~0u : 0u;
+        if ((dirty_in & D_W) && w == 0) b |= 1u;
+        if ((dirty_in & D_E) && w == TW / 32 - 1) b |= 1u << 31;
+        sm.dcol[w] = b;
+    }
+    if (threadIdx.x == 0) {
+        sm.edges = 0;
+        sm.sweeps = 0;
     }
     __syncthreads();
     for (int i = threadIdx.x; i < TW; i += NW * 32) {
@@ -505,63 +349,100 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
     bool anych = false;
     const int vr = rows - y0, vc = cols - x0;  // valid extent of this tile
     for (int it = 0; it < 1024; ++it) {
-        bool ch = false;
-        // ---- row phase
-        for (int r = warp; r < TH; r += NW) {
-            T *row = o + (r + 1) * P + 1;
-            const T *up = row - P, *dn = row + P;
-            T lo[KX], hi[KX], cur[KX], res[KX];
+        // ---- row phase over the dirty rows (round robin over warps)
+        unsigned rm[TH / 32];
 #pragma unroll
-            for (int k = 0; k < KX; ++k) {
-                int x = lane * KX + k;
-                cur[k] = row[x];
-                T w = smax(cur[k], smax(up[x], dn[x]));
-                if (conn8) w = smax(w, smax(smax(up[x - 1], up[x + 1]), smax(dn[x - 1], dn[x + 1])));
-                T mk = sm.m[r * TW + x];
-                bool in = r < vr && x < vc;
-                lo[k] = in ? smin(w, mk) : (T)0;
-                hi[k] = in ? mk : (T)0;
-            }
-            line_scan<T, KX>(lo, hi, row[-1], row[TW], res);
-#pragma unroll
-            for (int k = 0; k < KX; ++k) {
-                int x = lane * KX + k;
-                if (!(res[k] == cur[k])) {
-                    row[x] = res[k];
-                    ch = true;
-                }
-            }
-        }
+        for (int w = 0; w < TH / 32; ++w) rm[w] = sm.drow[w];
         __syncthreads();
-        // ---- column phase
-        for (int cidx = warp; cidx < TW; cidx += NW) {
-            T lo[KY], hi[KY], cur[KY], res[KY];
+        if (threadIdx.x < TH / 32) sm.drow[threadIdx.x] = 0;
+        bool chr = false;
+        int seq = 0;
 #pragma unroll
-            for (int k = 0; k < KY; ++k) {
-                int y = lane * KY + k;
-                T *p = o + (y + 1) * P + (cidx + 1);
-                cur[k] = p[0];
-                T w = smax(cur[k], smax(p[-1], p[1]));
-                if (conn8) w = smax(w, smax(smax(p[-P - 1], p[-P + 1]), smax(p[P - 1], p[P + 1])));
-                T mk = sm.m[y * TW + cidx];
-                bool in = y < vr && cidx < vc;
-                lo[k] = in ? smin(w, mk) : (T)0;
-                hi[k] = in ? mk : (T)0;
-            }
-            line_scan<T, KY>(lo, hi, o[cidx + 1], o[(TH + 1) * P + cidx + 1], res);
+        for (int w = 0; w < TH / 32; ++w) {
+            unsigned bits = rm[w];
+            while (bits) {
+                const int r = w * 32 + __ffs(bits) - 1;
+                bits &= bits - 1;
+                if ((seq++ & (NW - 1)) != warp) continue;
+                T *row = o + (r + 1) * P + 1;
+                const T *up = row - P, *dn = row + P;
+                T lo[KX], hi[KX], cur[KX], res[KX];
 #pragma unroll
-            for (int k = 0; k < KY; ++k) {
-                int y = lane * KY + k;
-                if (!(res[k] == cur[k])) {
-                    o[(y + 1) * P + cidx + 1] = res[k];
-                    ch = true;
+                for (int k = 0; k < KX; ++k) {
+                    int x = lane * KX + k;
+                    cur[k] = row[x];
+                    T w8 = smax(cur[k], smax(up[x], dn[x]));
+                    if (conn8) w8 = smax(w8, smax(smax(up[x - 1], up[x + 1]), smax(dn[x - 1], dn[x + 1])));
+                    T mk = sm.m[r * TW + x];
+                    bool in = r < vr && x < vc;
+                    lo[k] = in ? smin(w8, mk) : (T)0;
+                    hi[k] = in ? mk : (T)0;
+                }
+                line_scan<T, KX>(lo, hi, row[-1], row[TW], res);
+                unsigned changed = 0;
+#pragma unroll
+                for (int k = 0; k < KX; ++k) {
+                    int x = lane * KX + k;
+                    if (!(res[k] == cur[k])) {
+                        row[x] = res[k];
+                        changed |= 1u << k;
+                    }
+                }
+                if (__any_sync(0xffffffffu, changed != 0)) {
+                    chr = true;
+                    mark_dirty<KX, TW>(sm.dcol, changed);
                 }
             }
         }
-        const bool any = __syncthreads_or(ch);
+        chr = __syncthreads_or(chr);
+        // ---- column phase over the dirty columns
+        unsigned cm[TW / 32];
+#pragma unroll
+        for (int w = 0; w < TW / 32; ++w) cm[w] = sm.dcol[w];
+        __syncthreads();
+        if (threadIdx.x < TW / 32) sm.dcol[threadIdx.x] = 0;
+        bool chc = false;
+        seq = 0;
+#pragma unroll
+        for (int w = 0; w < TW / 32; ++w) {
+            unsigned bits = cm[w];
+            while (bits) {
+                const int cidx = w * 32 + __ffs(bits) - 1;
+                bits &= bits - 1;
+                if ((seq++ & (NW - 1)) != warp) continue;
+                T lo[KY], hi[KY], cur[KY], res[KY];
+#pragma unroll
+                for (int k = 0; k < KY; ++k) {
+                    int y = lane * KY + k;
+                    T *p = o + (y + 1) * P + (cidx + 1);
+                    cur[k] = p[0];
+                    T w8 = smax(cur[k], smax(p[-1], p[1]));
+                    if (conn8) w8 = smax(w8, smax(smax(p[-P - 1], p[-P + 1]), smax(p[P - 1], p[P + 1])));
+                    T mk = sm.m[y * TW + cidx];
+                    bool in = y < vr && cidx < vc;
+                    lo[k] = in ? smin(w8, mk) : (T)0;
+                    hi[k] = in ? mk : (T)0;
+                }
+                line_scan<T, KY>(lo, hi, o[cidx + 1], o[(TH + 1) * P + cidx + 1], res);
+                unsigned changed = 0;
+#pragma unroll
+                for (int k = 0; k < KY; ++k) {
+                    int y = lane * KY + k;
+                    if (!(res[k] == cur[k])) {
+                        o[(y + 1) * P + cidx + 1] = res[k];
+                        changed |= 1u << k;
+                    }
+                }
+                if (__any_sync(0xffffffffu, changed != 0)) {
+                    chc = true;
+                    mark_dirty<KY, TH>(sm.drow, changed);
+                }
+            }
+        }
+        chc = __syncthreads_or(chc);
         if (threadIdx.x == 0) sm.sweeps = it + 1;
-        if (!any) break;
-        anych = true;
+        anych = anych || chr || chc;
+        if (!chc) break;  // no row is dirty: the tile is stable
         if (it == 1023) my_edges |= 16u;  // not stable yet: process again later
     }
     // A neighbour tile needs another pass only if an edge pixel that changed
@@ -629,8 +510,14 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
     __syncthreads();
 }
 
+// lane 0 only: mark the neighbour's dirty edge, then queue it
+__device__ __forceinline__ void notify(Queue &q, int t, int bits) {
+    atomicOr(q.dirty + t, bits);
+    q_push(q, t);
+}
+
 template <typename T, int TW, int TH, int P>
-__global__ void __launch_bounds__(256) recon_cta(const T *__restrict__ mask, T *out, int rows, int cols, int conn,
+__global__ void __launch_bounds__(256, 2) recon_cta(const T *__restrict__ mask, T *out, int rows, int cols, int conn,
                                                  int tiles_x, int tiles_y, Queue q) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     TileSmem<T, TW, TH, P> &sm = *reinterpret_cast<TileSmem<T, TW, TH, P> *>(sm_raw);
@@ -643,19 +530,23 @@ __global__ void __launch_bounds__(256) recon_cta(const T *__restrict__ mask, T *
         if (t < 0) break;
         __threadfence();
         for (;;) {
+            if (threadIdx.x == 0) sm.dirty = atomicExch(q.dirty + t, 0);
+            __syncthreads();
+            const int dirty = sm.dirty;
             const int tx = t % tiles_x, ty = t / tiles_x;
-            cta_process_tile<T, TW, TH, P>(mask, out, rows, cols, conn8, tx, ty, sm);
+            cta_process_tile<T, TW, TH, P>(mask, out, rows, cols, conn8, tx, ty, dirty, sm);
             if (threadIdx.x == 0) {
-                unsigned edges = (unsigned)sm.edges;
-                if (edges & 16u) q_push(q, t);
-                if (edges & 1u && ty > 0) q_push(q, t - tiles_x);
-                if (edges & 2u && ty + 1 < tiles_y) q_push(q, t + tiles_x);
-                if (edges & 4u && tx > 0) q_push(q, t - 1);
-                if (edges & 8u && tx + 1 < tiles_x) q_push(q, t + 1);
-                if (edges & 32u && ty > 0 && tx > 0) q_push(q, t - tiles_x - 1);
-                if (edges & 64u && ty > 0 && tx + 1 < tiles_x) q_push(q, t - tiles_x + 1);
-                if (edges & 128u && ty + 1 < tiles_y && tx > 0) q_push(q, t + tiles_x - 1);
-                if (edges & 256u && ty + 1 < tiles_y && tx + 1 < tiles_x) q_push(q, t + tiles_x + 1);
+                const unsigned edges = (unsigned)sm.edges;
+                // our top edge is the upper tile's bottom halo, and so on
+                if (edges & 16u) notify(q, t, D_ALL);
+                if (edges & 1u && ty > 0) notify(q, t - tiles_x, D_S);
+                if (edges & 2u && ty + 1 < tiles_y) notify(q, t + tiles_x, D_N);
+                if (edges & 4u && tx > 0) notify(q, t - 1, D_E);
+                if (edges & 8u && tx + 1 < tiles_x) notify(q, t + 1, D_W);
+                if (edges & 32u && ty > 0 && tx > 0) notify(q, t - tiles_x - 1, D_S);
+                if (edges & 64u && ty > 0 && tx + 1 < tiles_x) notify(q, t - tiles_x + 1, D_S);
+                if (edges & 128u && ty + 1 < tiles_y && tx > 0) notify(q, t + tiles_x - 1, D_N);
+                if (edges & 256u && ty + 1 < tiles_y && tx + 1 < tiles_x) notify(q, t + tiles_x + 1, D_N);
                 atomicAdd(q.stats, 1);
                 atomicAdd(q.stats + 1, sm.sweeps);
                 sm.again = q_finish(q, t);
@@ -679,7 +570,8 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
     const int qcap = 2 * ntiles;
     int *state = c.ws.i32[5];
     int *queue = state + ntiles;
-    if ((int64_t)ntiles + qcap > c.max_pad) {
+    int *dirty = queue + qcap;
+    if (2 * (int64_t)ntiles + qcap > c.max_pad) {
         c.last_error = "tile queue does not fit";
         return NSG_ERR_OOM;
     }
@@ -691,7 +583,7 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
         init_min_f32<<<blocks, 256, 0, s>>>((const float *)marker, (const float *)mask, (float *)out, n);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
-    init_queue<<<(qcap + 255) / 256, 256, 0, s>>>(state, queue, qcap, ntiles, c.ws.ctrl);
+    init_queue<<<(qcap + 255) / 256, 256, 0, s>>>(state, queue, dirty, qcap, ntiles, c.ws.ctrl);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     Queue q;
@@ -703,6 +595,7 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
     q.outstanding = c.ws.ctrl + C_QPEND;
     q.status = c.ws.ctrl + C_STATUS;
     q.budget = c.spin_budget;
+    q.dirty = dirty;
     q.stats = c.ws.ctrl + C_RSTATS;
     const size_t smem = sizeof(TileSmem<T, TW, TH, P>);
     auto kfn = recon_cta<T, TW, TH, P>;
@@ -718,56 +611,6 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
     return NSG_SUCCESS;
 }
 
-template <typename T, int TH, int WARPS>
-int run_recon(Ctx &c, const T *marker, const T *mask, T *out, int rows, int cols, int conn, cudaStream_t s) {
-    NSG_TRY(check_dims(c, rows, cols));
-    NSG_TRY(check_conn(c, conn));
-    const int64_t n = (int64_t)rows * cols;
-    const int tiles_x = (cols + TW - 1) / TW, tiles_y = (rows + TH - 1) / TH;
-    const int ntiles = tiles_x * tiles_y;
-    const int qcap = 2 * ntiles;
-    int *state = c.ws.i32[5];
-    int *queue = state + ntiles;
-    if ((int64_t)ntiles + qcap > c.max_pad) {
-        c.last_error = "tile queue does not fit";
-        return NSG_ERR_OOM;
-    }
-    int blocks = (int)((n + 255) / 256);
-    if (blocks > c.sm_count * 16) blocks = c.sm_count * 16;
-    if (sizeof(T) == 1)
-        init_min_u8<<<blocks, 256, 0, s>>>((const uint8_t *)marker, (const uint8_t *)mask, (uint8_t *)out, n);
-    else
-        init_min_f32<<<blocks, 256, 0, s>>>((const float *)marker, (const float *)mask, (float *)out, n);
-    NSG_COUNT_LAUNCH();
-    NSG_LAUNCH_CHECK(c);
-    init_queue<<<(qcap + 255) / 256, 256, 0, s>>>(state, queue, qcap, ntiles, c.ws.ctrl);
-    NSG_COUNT_LAUNCH();
-    NSG_LAUNCH_CHECK(c);
-    Queue q;
-    q.state = state;
-    q.queue = queue;
-    q.qcap = qcap;
-    q.head = c.ws.ctrl + C_QHEAD;
-    q.tail = c.ws.ctrl + C_QTAIL;
-    q.outstanding = c.ws.ctrl + C_QPEND;
-    q.status = c.ws.ctrl + C_STATUS;
-    q.budget = c.spin_budget;
-    q.stats = c.ws.ctrl + C_RSTATS;
-    const size_t smem = (size_t)WARPS * ((TH + 2) * (TW + 2) + TH * TW) * sizeof(T);
-    auto kfn = recon_persistent<T, TH, WARPS>;
-    NSG_CUDA_TRY(c, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    NSG_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, WARPS * 32, smem));
-    if (per_sm < 1) per_sm = 1;
-    int grid = c.sm_count * per_sm;
-    int need = (ntiles + WARPS - 1) / WARPS;
-    if (grid > need) grid = need;
-    kfn<<<grid, WARPS * 32, smem, s>>>(mask, out, rows, cols, conn, tiles_x, tiles_y, q);
-    NSG_COUNT_LAUNCH();
-    NSG_LAUNCH_CHECK(c);
-    return NSG_SUCCESS;
-}
-
 }  // namespace
 
 int recon_u8(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t *out, int rows, int cols, int conn,
@@ -778,16 +621,6 @@ int recon_u8(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t *out, i
 int recon_f32(Ctx &c, const float *marker, const float *mask, float *out, int rows, int cols, int conn,
               cudaStream_t s) {
     return run_recon_cta<float, 64, 64, 67>(c, marker, mask, out, rows, cols, conn, s);
-}
-
-// the warp-per-tile variant (kept for comparison)
-int recon_u8_warp(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t *out, int rows, int cols, int conn,
-                  cudaStream_t s) {
-    return run_recon<uint8_t, 64, 4>(c, marker, mask, out, rows, cols, conn, s);
-}
-int recon_f32_warp(Ctx &c, const float *marker, const float *mask, float *out, int rows, int cols, int conn,
-                   cudaStream_t s) {
-    return run_recon<float, 32, 4>(c, marker, mask, out, rows, cols, conn, s);
 }
 
 }  // namespace nsg

@@ -41,6 +41,7 @@
 // watershed-labelled first U pixel, an unowned active shell, an overflow) a
 // device flag makes the serial flood (ws_flood_serial) produce the result.
 #include <limits.h>
+#include <stdlib.h>
 
 #include <cooperative_groups.h>
 
@@ -598,13 +599,16 @@ __global__ void __launch_bounds__(kBfsThreads, 1) k_bfs(PW a, const uint8_t *__r
     const int off[4] = {-1, 1, -W, W};
     int prevcap = 1, base = 0, layer = 0;
     for (;;) {
-        if (threadIdx.x == 0) {
-            int acc = 0;
-            for (int j = 0; j < C; ++j) {
-                offs[j] = acc;
-                acc += *cl.map_shared_rank(&tot, j);
+        if (threadIdx.x < 32) {  // every CTA's count, read in parallel, then a warp scan
+            const int lane = threadIdx.x;
+            const int v = lane < C ? *cl.map_shared_rank(&tot, lane) : 0;
+            int x = v;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, d);
+                if (lane >= d) x += y;
             }
-            offs[C] = acc;
+            if (lane <= C) offs[lane] = x - v;  // exclusive prefix; offs[C] = total
         }
         __syncthreads();
         const int s = offs[C];
@@ -1294,6 +1298,10 @@ static int launch_bfs(Ctx &c, const PW &a, const uint8_t *nbm, cudaStream_t s) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int cl = kBfsMaxCluster;
+    if (const char *e = getenv("NSG_BFS_CLUSTER")) {  // tuning knob: largest cluster to try
+        const int v = atoi(e);
+        if (v >= 1 && v <= kBfsMaxCluster) cl = v;
+    }
     for (; cl > 1; cl /= 2) {
         cfg.gridDim = dim3(cl);
         attr[0].val.clusterDim.x = cl;
