@@ -25,6 +25,7 @@ import os
 import statistics
 import subprocess
 import sys
+import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -46,6 +47,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="nsg", choices=["nsg", "reference"])
     ap.add_argument("--tiles", type=int, default=256)
+    ap.add_argument("--streams", type=int, default=8,
+                    help="tiles in flight: host threads, each with its own context and CUDA stream")
     ap.add_argument("--cpu-sample-tiles", type=int, default=0, help="tiles in the CPU baseline sample (0 = cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -205,60 +208,108 @@ def run_nsg(args, rank, world, local):
     tiles = make_batch(args.tiles, 0x5EED0003 + 100003 * rank, dev)
     maxr = max(t.shape[0] for t in tiles)
     maxc = max(t.shape[1] for t in tiles)
-    ctx = Context(maxr, maxc, local)
-    stream = torch.cuda.Stream(device=dev)
-    sh = C.c_void_p(stream.cuda_stream)
     px = sum(t.shape[0] * t.shape[1] for t in tiles)
-    labels = torch.empty(maxr * maxc, dtype=torch.int32, device=dev)
-    cc = C.c_int(0)
     params = _lib.SegParams()
     statuses = {}
     tile_ms = []
 
-    def step(record_latency=False):
-        for t in tiles:
-            r, c = t.shape[0], t.shape[1]
-            t0 = time.perf_counter()
-            st = L.nsg_segment_nuclei(ctx.h, ptr(t), r, c, c * 3, C.byref(params), ptr(labels), None,
-                                      C.byref(cc), None, sh)
-            if st < 0:
-                raise _lib.NsgError(st, ctx.last_error())
-            if record_latency:
-                stream.synchronize()
-                tile_ms.append((time.perf_counter() - t0) * 1e3)
-                statuses[st] = statuses.get(st, 0) + 1
+    class Worker:
+        """One tile in flight: a context (workspace arena), a stream, label buffers."""
+
+        def __init__(self):
+            self.ctx = Context(maxr, maxc, local)
+            self.stream = torch.cuda.Stream(device=dev)
+            self.sh = C.c_void_p(self.stream.cuda_stream)
+            self.labels = torch.empty(maxr * maxc, dtype=torch.int32, device=dev)
+            self.host_lab = None
+            self.cc = C.c_int(0)
+
+    workers = [Worker() for _ in range(max(1, args.streams))]
+
+    def run_tiles(fn, items, pool):
+        """Hand `items` to the workers of `pool` (one host thread each) until all are done."""
+        nxt = [0]
+        lock = threading.Lock()
+        errors = []
+
+        def loop(w):
+            try:
+                with torch.cuda.stream(w.stream):
+                    while True:
+                        with lock:
+                            i = nxt[0]
+                            nxt[0] += 1
+                        if i >= len(items):
+                            return
+                        fn(w, items[i])
+            except Exception as e:  # noqa: BLE001 - re-raised on the main thread
+                errors.append(e)
+
+        ths = [threading.Thread(target=loop, args=(w,)) for w in pool]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        if errors:
+            raise errors[0]
+
+    def seg_device(w, t, record_latency=False):
+        r, c = t.shape[0], t.shape[1]
+        t0 = time.perf_counter()
+        st = L.nsg_segment_nuclei(w.ctx.h, ptr(t), r, c, c * 3, C.byref(params), ptr(w.labels), None,
+                                  C.byref(w.cc), None, w.sh)
+        if st < 0:
+            raise _lib.NsgError(st, w.ctx.last_error())
+        if record_latency:
+            w.stream.synchronize()
+            tile_ms.append((time.perf_counter() - t0) * 1e3)
+            statuses[st] = statuses.get(st, 0) + 1
 
     def barrier():
         if world > 1:
             import torch.distributed as dist
             dist.barrier()
 
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            step()
-        stream.synchronize()
-        L.nsg_context_set_timing(ctx.h, 1)
-        barrier()
-        launches0 = L.nsg_kernel_launches()
-        with Clocks(local) as clk:
-            torch.cuda.synchronize()
-            ev0 = torch.cuda.Event(enable_timing=True)
-            ev1 = torch.cuda.Event(enable_timing=True)
-            ev0.record(stream)
-            for _ in range(args.steps):
-                step()
-            ev1.record(stream)
-            torch.cuda.synchronize()
-        launches = L.nsg_kernel_launches() - launches0
-        barrier()
-        total_ms = ev0.elapsed_time(ev1)
-        stage_ms = (C.c_double * 19)()
+    main = torch.cuda.current_stream(dev)
+
+    def timed(fn, items, n_steps):
+        """CUDA-event time of n_steps passes over `items` on all workers."""
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(main)
+        for w in workers:
+            w.stream.wait_event(ev0)
+        for _ in range(n_steps):
+            run_tiles(fn, items, workers)
+        for w in workers:
+            main.wait_stream(w.stream)
+        ev1.record(main)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1)
+
+    for _ in range(args.warmup):
+        run_tiles(seg_device, tiles, workers)
+    torch.cuda.synchronize()
+    for w in workers:
+        L.nsg_context_set_timing(w.ctx.h, 1)
+    barrier()
+    launches0 = L.nsg_kernel_launches()
+    with Clocks(local) as clk:
+        total_ms = timed(seg_device, tiles, args.steps)
+    launches = L.nsg_kernel_launches() - launches0
+    barrier()
+    stage_ms = [0.0] * 19
+    for w in workers:
+        sm = (C.c_double * 19)()
         calls = C.c_longlong(0)
-        L.nsg_context_stage_times(ctx.h, stage_ms, 19, C.byref(calls))
-        L.nsg_context_set_timing(ctx.h, 0)
-        names = [L.nsg_stage_name(i).decode() for i in range(19)]
-        # per-tile latency (separate pass, synchronised per tile)
-        step(record_latency=True)
+        L.nsg_context_stage_times(w.ctx.h, sm, 19, C.byref(calls))
+        L.nsg_context_set_timing(w.ctx.h, 0)
+        for i in range(19):
+            stage_ms[i] += sm[i]
+    names = [L.nsg_stage_name(i).decode() for i in range(19)]
+    # per-tile latency: one tile at a time on one worker (separate pass)
+    run_tiles(lambda w, t: seg_device(w, t, record_latency=True), tiles, workers[:1])
     ms_step = total_ms / args.steps
     value_rank = px / (ms_step / 1e3) / 1e6
     if world > 1:
@@ -276,26 +327,27 @@ def run_nsg(args, rank, world, local):
     peak, peak_kind = peaks()
     achieved = dom_bytes / (dom_ms_per_step / 1e3) / 1e9 if dom_ms_per_step > 0 else 0.0
 
-    # e2e: host (pinned) tiles through the public host entry point, labels read back
+    # e2e: host (pinned) tiles through the public host entry point, labels read
+    # back to pinned host memory; copies both ways inside the timed region
     e2e_tiles = tiles[: min(len(tiles), 64)]
     host_in = [t.cpu().pin_memory() for t in e2e_tiles]
-    host_lab = torch.empty(maxr * maxc, dtype=torch.int32).pin_memory()
+    for w in workers:
+        w.host_lab = torch.empty(maxr * maxc, dtype=torch.int32).pin_memory()
     e2e_px = sum(t.shape[0] * t.shape[1] for t in e2e_tiles)
 
-    def e2e_step():
-        for h in host_in:
-            r, c = h.shape[0], h.shape[1]
-            st = L.nsg_segment_nuclei_host(ctx.h, C.c_void_p(h.data_ptr()), r, c, C.byref(params),
-                                           C.c_void_p(host_lab.data_ptr()), None, C.byref(cc), None, sh)
-            if st < 0:
-                raise _lib.NsgError(st, ctx.last_error())
+    def seg_host(w, h):
+        r, c = h.shape[0], h.shape[1]
+        st = L.nsg_segment_nuclei_host(w.ctx.h, C.c_void_p(h.data_ptr()), r, c, C.byref(params),
+                                       C.c_void_p(w.host_lab.data_ptr()), None, C.byref(w.cc), None, w.sh)
+        if st < 0:
+            raise _lib.NsgError(st, w.ctx.last_error())
 
-    e2e_step()
-    stream.synchronize()
+    run_tiles(seg_host, host_in, workers)
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        e2e_step()
-    stream.synchronize()
+        run_tiles(seg_host, host_in, workers)
+    torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_value = world * e2e_px / e2e_s / 1e6
 
@@ -319,8 +371,10 @@ def run_nsg(args, rank, world, local):
         "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "config": {"workload": f"segmentNuclei over {len(tiles)} uneven synthetic H&E tiles "
-                               f"(squares 512-4096 + ragged edge tiles), per-tile calls, device-resident inputs",
-                   "tiles": len(tiles), "pixels_per_step": px, "form": "per-tile",
+                               f"(squares 512-4096 + ragged edge tiles), device-resident inputs",
+                   "tiles": len(tiles), "pixels_per_step": px,
+                   "form": f"per-tile calls, {len(workers)} tiles in flight (host threads, one context and "
+                           f"stream each)",
                    "l2": "inputs larger than L2 (5.6 GB per step)", "parallelism": f"replicas x{world}"},
         "latency_ms": {"p50": round(lat[len(lat) // 2], 3), "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3)},
         "statuses": {str(k): v for k, v in statuses.items()},

@@ -249,6 +249,12 @@ namespace {
 
 inline cudaStream_t S(nsg_stream_t s) { return (cudaStream_t)s; }
 
+// device -> host copy ordered on the caller's stream (never the legacy stream)
+cudaError_t copy_to_host(void *dst, const void *src, size_t bytes, cudaStream_t s) {
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
+    return e == cudaSuccess ? cudaStreamSynchronize(s) : e;
+}
+
 // Every per-operation entry point resets the device status word, enqueues
 // its kernels and synchronises the stream, returning the device status: the
 // reference's calls return finished results, and spinning kernels report
@@ -275,8 +281,7 @@ int nsg_get_background(nsg_context *h, const uint8_t *bgr, int rows, int cols, i
         return background_count(c, bgr, (int64_t)cols * 3, rows, cols, blue, green, red, mask_out, c.ws.ctr64, S(s));
     });
     if (r == NSG_SUCCESS && count_out) {
-        if (cudaMemcpy(count_out, h->c.ws.ctr64, sizeof(int64_t), cudaMemcpyDeviceToHost) != cudaSuccess)
-            return NSG_ERR_CUDA;
+        if (copy_to_host(count_out, h->c.ws.ctr64, sizeof(int64_t), S(s)) != cudaSuccess) return NSG_ERR_CUDA;
     }
     return r;
 }
@@ -398,8 +403,7 @@ int nsg_bwareaopen(nsg_context *h, const uint8_t *img, uint8_t *out, int rows, i
         return bwareaopen_dev(c, img, out, rows, cols, min_size, max_size, conn, c.ws.ctrl + C_COUNT1, S(s));
     });
     if (r == NSG_SUCCESS && count_out) {
-        if (cudaMemcpy(count_out, h->c.ws.ctrl + C_COUNT1, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
-            return NSG_ERR_CUDA;
+        if (copy_to_host(count_out, h->c.ws.ctrl + C_COUNT1, sizeof(int), S(s)) != cudaSuccess) return NSG_ERR_CUDA;
     }
     return r;
 }
@@ -477,15 +481,14 @@ int nsg_bounding_box(nsg_context *h, const int32_t *labels, int rows, int cols, 
     if (r != NSG_SUCCESS) return r;
     Ctx &c = h->c;
     int cnt = 0;
-    if (cudaMemcpy(&cnt, c.ws.ctrl + C_COUNT0, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return NSG_ERR_CUDA;
+    if (copy_to_host(&cnt, c.ws.ctrl + C_COUNT0, sizeof(int), S(s)) != cudaSuccess) return NSG_ERR_CUDA;
     if (compcount) *compcount = cnt;
     if (bbox_out) {
         if (cnt > capacity) {
             c.last_error = "bbox capacity too small";
             return NSG_ERR_ARG;
         }
-        if (cnt > 0 && cudaMemcpy(bbox_out, c.ws.p_i32[1], sizeof(int32_t) * 5 * (size_t)cnt,
-                                  cudaMemcpyDeviceToHost) != cudaSuccess)
+        if (cnt > 0 && copy_to_host(bbox_out, c.ws.p_i32[1], sizeof(int32_t) * 5 * (size_t)cnt, S(s)) != cudaSuccess)
             return NSG_ERR_CUDA;
     }
     return NSG_SUCCESS;
