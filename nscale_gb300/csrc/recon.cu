@@ -28,6 +28,7 @@
 //    bounded by the context's spin budget and reports NSG_ERR_TIMEOUT.
 #include <float.h>
 #include <math.h>
+#include <stdlib.h>
 
 #include "nsg_internal.cuh"
 
@@ -118,15 +119,21 @@ struct Queue {
     int *dirty;  // per tile: D_* bits for its next pass
     int *stats;  // [0] tile passes, [1] row+column sweeps
     long long budget;
+    int idle_limit;  // empty-queue polls before an idle CTA leaves (0: stay until done)
 };
 
 // lane 0 only
+// An idle CTA may leave while other CTAs still hold tiles: a CTA that queues
+// a tile always comes back here and takes it if nobody else does, so every
+// queued tile is processed; leaving early hands the SM to other streams.
 __device__ int q_pop(Queue &q) {
     long long spins = 0;
+    int idle = 0;
     for (;;) {
         int h = *(volatile int *)q.head;
         int tl = *(volatile int *)q.tail;
         if (h < tl) {
+            idle = 0;
             if (atomicCAS(q.head, h, h + 1) == h) {
                 int slot = h % q.qcap;
                 int v;
@@ -146,6 +153,7 @@ __device__ int q_pop(Queue &q) {
             continue;
         }
         if (atomicAdd(q.outstanding, 0) == 0) return -1;
+        if (q.idle_limit > 0 && ++idle > q.idle_limit) return -1;
         if (*(volatile int *)q.status & DEV_TIMEOUT) return -2;
         if (++spins > q.budget) {
             atomicOr(q.status, DEV_TIMEOUT);
@@ -596,14 +604,25 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
     q.status = c.ws.ctrl + C_STATUS;
     q.budget = c.spin_budget;
     q.dirty = dirty;
+    q.idle_limit = 2048;
+    if (const char *e = getenv("NSG_RECON_IDLE")) q.idle_limit = atoi(e);  // tuning knob
     q.stats = c.ws.ctrl + C_RSTATS;
     const size_t smem = sizeof(TileSmem<T, TW, TH, P>);
     auto kfn = recon_cta<T, TW, TH, P>;
     NSG_CUDA_TRY(c, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     NSG_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, 256, smem));
+    // One CTA per SM by default: the work is CTA-throughput bound and a second
+    // CTA per SM mostly takes room that concurrent streams' kernels can use.
+    int want = 1;
+    if (const char *e = getenv("NSG_RECON_CTAS_PER_SM")) want = atoi(e);  // tuning knob
+    if (want >= 1 && want < per_sm) per_sm = want;
     if (per_sm < 1) per_sm = 1;
     int grid = c.sm_count * per_sm;
+    if (const char *e = getenv("NSG_RECON_MAX_CTAS")) {  // tuning knob: cap on the persistent grid
+        const int v = atoi(e);
+        if (v >= 1 && v < grid) grid = v;
+    }
     if (grid > ntiles) grid = ntiles;
     kfn<<<grid, 256, smem, s>>>(mask, out, rows, cols, conn, tiles_x, tiles_y, q);
     NSG_COUNT_LAUNCH();
