@@ -157,6 +157,7 @@ int nsg_context_destroy(nsg_context *h) {
     Ctx &c = h->c;
     cudaSetDevice(c.device);
     cudaDeviceSynchronize();
+    if (c.ev_counts) cudaEventDestroy(c.ev_counts);
     if (c.ws.h_ctrl) cudaFreeHost(c.ws.h_ctrl);
     if (c.ws.h_ctr64) cudaFreeHost(c.ws.h_ctr64);
     if (c.arena) cudaFree(c.arena);

@@ -90,6 +90,7 @@ struct Ctx {
     Workspace ws;
     int sm_count = 0;
     long long spin_budget = 1ll << 26;
+    cudaEvent_t ev_counts = nullptr;  // marks a posted readback of the device counters
     std::string last_error;
 };
 

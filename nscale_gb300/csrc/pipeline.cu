@@ -48,10 +48,22 @@ void disk19(uint8_t *se) {
 // getStructuringElement(MORPH_ELLIPSE, Size(3,3)) = 3x3 cross
 const uint8_t kCross3[9] = {0, 1, 0, 1, 1, 1, 0, 1, 0};
 
-int read_counts(Ctx &c, cudaStream_t s) {
+// The pipeline's three decisions need device counters on the host.  Instead
+// of draining the stream at each one, the readback is posted (copy + event)
+// and the host keeps enqueuing the next stages, which are harmless on a tile
+// that turns out to be background or empty; it waits for the event only
+// where a decision must be taken, so the stream rarely runs dry.
+int post_counts(Ctx &c, cudaStream_t s) {
+    if (!c.ev_counts) NSG_CUDA_TRY(c, cudaEventCreateWithFlags(&c.ev_counts, cudaEventDisableTiming));
     NSG_CUDA_TRY(c, cudaMemcpyAsync(c.ws.h_ctrl, c.ws.ctrl, 8 * sizeof(int), cudaMemcpyDeviceToHost, s));
     NSG_CUDA_TRY(c, cudaMemcpyAsync(c.ws.h_ctr64, c.ws.ctr64, 4 * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    NSG_CUDA_TRY(c, cudaStreamSynchronize(s));
+    NSG_CUDA_TRY(c, cudaEventRecord(c.ev_counts, s));
+    return NSG_SUCCESS;
+}
+
+// wait for the last posted readback and check the device status word
+int take_counts(Ctx &c) {
+    NSG_CUDA_TRY(c, cudaEventSynchronize(c.ev_counts));
     int st = c.ws.h_ctrl[C_STATUS];
     if (st & DEV_QUEUE_FULL) {
         c.last_error = "device queue overflow";
@@ -143,12 +155,7 @@ int segment_nuclei_dev(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int
     NSG_TRY(background_count(c, bgr, stride, rows, cols, p.blue, p.green, p.red, nullptr, c.ws.ctr64, s));
     NSG_TRY(front_rbc(c, bgr, stride, rows, cols, p.T1, p.T2, P[0], P[1], P[2], P[3], ctrl + C_COUNT0, s));
     t_mark(c, 0, s);
-    NSG_TRY(read_counts(c, s));
-    {
-        float ratio = (float)c.ws.h_ctr64[0] / (float)n;  // HE:125-126
-        if (ratio >= 0.99) return fail_fill(NSG_BACKGROUND);
-        if (ratio >= 0.9) return fail_fill(NSG_BACKGROUND_LIKELY);
-    }
+    NSG_TRY(post_counts(c, s));  // background ratio, decided after the reconstruction is enqueued
     // rbc = bwselect(bw2, bw1, 8) & imR2B (no seeds -> all zero, HE:73-79)
     NSG_TRY(bwselect_dev(c, P[2], P[1], P[4], rows, cols, 8, s));
     and_u8<<<g, kB, 0, s>>>(P[4], P[3], n);
@@ -166,14 +173,19 @@ int segment_nuclei_dev(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int
     // diffIm > G1, diffIm > G2
     NSG_TRY(diff_threshold(c, P[0], P[7], rows, cols, p.G1, p.G2, P[5], P[8], s));
     t_mark(c, 3, s);
+    NSG_TRY(take_counts(c));
+    {
+        float ratio = (float)c.ws.h_ctr64[0] / (float)n;  // HE:125-126
+        if (ratio >= 0.99) return fail_fill(NSG_BACKGROUND);
+        if (ratio >= 0.9) return fail_fill(NSG_BACKGROUND_LIKELY);
+    }
     // bw1 = imfillHoles(diffIm > G1, fillHolesConnectivity)
     NSG_TRY(fill_holes_dev(c, P[5], P[6], rows, cols, p.fillHolesConnectivity, s));
     t_mark(c, 4, s);
     // bw1_t = bwareaopen2(bw1, minSize, maxSize, 8)
     NSG_TRY(bwareaopen_dev(c, P[6], P[7], rows, cols, p.minSize, p.maxSize, 8, ctrl + C_COUNT1, s));
     t_mark(c, 5, s);
-    NSG_TRY(read_counts(c, s));
-    if (c.ws.h_ctrl[C_COUNT1] == 0) return fail_fill(NSG_NO_CANDIDATES_LEFT);
+    NSG_TRY(post_counts(c, s));  // candidates left?  decided before the watershed
     // seg_norbc = bwselect(diffIm > G2, bw1_t, 8) & (rbc == 0)
     NSG_TRY(bwselect_dev(c, P[8], P[7], P[5], rows, cols, 8, s));
     NSG_TRY(and_not(c, P[5], P[4], n, s));
@@ -196,6 +208,8 @@ int segment_nuclei_dev(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int
     t_mark(c, 11, s);
     NSG_TRY(imhmin_dev(c, c.ws.p_f32[1], c.ws.p_f32[0], rows, cols, 1.0f, 8, s));  // HE:384 (hard-coded 8)
     t_mark(c, 12, s);
+    NSG_TRY(take_counts(c));
+    if (c.ws.h_ctrl[C_COUNT1] == 0) return fail_fill(NSG_NO_CANDIDATES_LEFT);
     uint8_t *nuclei = (uint8_t *)c.ws.p_i32[0];
     NSG_TRY(mask_copy_bgr(c, bgr, stride, P[6], rows, cols, nuclei, s));
     NSG_TRY(watershed_dev(c, nuclei, c.ws.p_f32[0], c.ws.p_i32[1], rows, cols, p.watershedConnectivity, s));
@@ -207,19 +221,22 @@ int segment_nuclei_dev(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int
     // ---- final area filter, fill, label, boxes ------------------------------------
     NSG_TRY(bwareaopen_dev(c, P[7], P[8], rows, cols, p.minSizeSeg, p.maxSizeSeg, 4, ctrl + C_COUNT3, s));
     t_mark(c, 14, s);
-    NSG_TRY(read_counts(c, s));
-    if (c.ws.h_ctrl[C_COUNT3] == 0) return fail_fill(NSG_NO_CANDIDATES_LEFT);
+    // the last decision (any nuclei left?) is read together with the box count
     uint8_t *fin = mask_out ? mask_out : P[9];
     NSG_TRY(fill_holes_dev(c, P[8], fin, rows, cols, p.fillHolesConnectivity, s));
     t_mark(c, 15, s);
     int32_t *labels = labels_out ? labels_out : c.ws.p_i32[0];
     NSG_TRY(bwlabel_dev(c, fin, labels, rows, cols, 8, s));
     t_mark(c, 16, s);
+    int32_t *d_bbox = c.ws.p_i32[1];
     if (compcount || bbox) {
-        int32_t *d_bbox = c.ws.p_i32[1];
         NSG_TRY(bbox_dev(c, labels, rows, cols, d_bbox, c.max_pad, ctrl + C_COUNT0, s));
         t_mark(c, 17, s);
-        NSG_TRY(read_counts(c, s));
+    }
+    NSG_TRY(post_counts(c, s));
+    NSG_TRY(take_counts(c));
+    if (c.ws.h_ctrl[C_COUNT3] == 0) return fail_fill(NSG_NO_CANDIDATES_LEFT);
+    if (compcount || bbox) {
         int cnt = c.ws.h_ctrl[C_COUNT0];
         if (compcount) *compcount = cnt;
         if (bbox) {

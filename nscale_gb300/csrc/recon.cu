@@ -295,10 +295,9 @@ __device__ __forceinline__ void line_scan(T (&lo)[K], T (&hi)[K], T first, T las
 // One pass over tile (tx, ty): load, alternate row / column phases over the
 // dirty lines until nothing changes, report which neighbours must run again,
 // write back.
-template <typename T, int TW, int TH, int P>
+template <typename T, int TW, int TH, int P, int NW>
 __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, int cols, bool conn8, int tx, int ty,
                                  int dirty_in, TileSmem<T, TW, TH, P> &sm) {
-    constexpr int NW = 8;
     constexpr int KX = TW / 32, KY = TH / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int y0 = ty * TH, x0 = tx * TW;
@@ -524,8 +523,8 @@ __device__ __forceinline__ void notify(Queue &q, int t, int bits) {
     q_push(q, t);
 }
 
-template <typename T, int TW, int TH, int P>
-__global__ void __launch_bounds__(256, 2) recon_cta(const T *__restrict__ mask, T *out, int rows, int cols, int conn,
+template <typename T, int TW, int TH, int P, int NW>
+__global__ void __launch_bounds__(NW * 32, NW >= 16 ? 1 : 2) recon_cta(const T *__restrict__ mask, T *out, int rows, int cols, int conn,
                                                  int tiles_x, int tiles_y, Queue q) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     TileSmem<T, TW, TH, P> &sm = *reinterpret_cast<TileSmem<T, TW, TH, P> *>(sm_raw);
@@ -542,7 +541,7 @@ __global__ void __launch_bounds__(256, 2) recon_cta(const T *__restrict__ mask, 
             __syncthreads();
             const int dirty = sm.dirty;
             const int tx = t % tiles_x, ty = t / tiles_x;
-            cta_process_tile<T, TW, TH, P>(mask, out, rows, cols, conn8, tx, ty, dirty, sm);
+            cta_process_tile<T, TW, TH, P, NW>(mask, out, rows, cols, conn8, tx, ty, dirty, sm);
             if (threadIdx.x == 0) {
                 const unsigned edges = (unsigned)sm.edges;
                 // our top edge is the upper tile's bottom halo, and so on
@@ -568,7 +567,7 @@ __global__ void __launch_bounds__(256, 2) recon_cta(const T *__restrict__ mask, 
     }
 }
 
-template <typename T, int TW, int TH, int P>
+template <typename T, int TW, int TH, int P, int NW>
 int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int cols, int conn, cudaStream_t s) {
     NSG_TRY(check_dims(c, rows, cols));
     NSG_TRY(check_conn(c, conn));
@@ -608,10 +607,10 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
     if (const char *e = getenv("NSG_RECON_IDLE")) q.idle_limit = atoi(e);  // tuning knob
     q.stats = c.ws.ctrl + C_RSTATS;
     const size_t smem = sizeof(TileSmem<T, TW, TH, P>);
-    auto kfn = recon_cta<T, TW, TH, P>;
+    auto kfn = recon_cta<T, TW, TH, P, NW>;
     NSG_CUDA_TRY(c, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    NSG_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, 256, smem));
+    NSG_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, NW * 32, smem));
     // One CTA per SM by default: the work is CTA-throughput bound and a second
     // CTA per SM mostly takes room that concurrent streams' kernels can use.
     int want = 1;
@@ -624,22 +623,37 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
         if (v >= 1 && v < grid) grid = v;
     }
     if (grid > ntiles) grid = ntiles;
-    kfn<<<grid, 256, smem, s>>>(mask, out, rows, cols, conn, tiles_x, tiles_y, q);
+    kfn<<<grid, NW * 32, smem, s>>>(mask, out, rows, cols, conn, tiles_x, tiles_y, q);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
+}
+
+// warps per tile CTA
+int recon_warps() {
+    if (const char *e = getenv("NSG_RECON_WARPS")) {  // tuning knob: 8, 16 or 32
+        const int v = atoi(e);
+        if (v == 8 || v == 16 || v == 32) return v;
+    }
+    return 8;  // more warps shorten one reconstruction but crowd out concurrent tiles
 }
 
 }  // namespace
 
 int recon_u8(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t *out, int rows, int cols, int conn,
              cudaStream_t s) {
-    return run_recon_cta<uint8_t, 128, 128, 132>(c, marker, mask, out, rows, cols, conn, s);
+    const int nw = recon_warps();
+    if (nw == 8) return run_recon_cta<uint8_t, 128, 128, 132, 8>(c, marker, mask, out, rows, cols, conn, s);
+    if (nw == 32) return run_recon_cta<uint8_t, 128, 128, 132, 32>(c, marker, mask, out, rows, cols, conn, s);
+    return run_recon_cta<uint8_t, 128, 128, 132, 16>(c, marker, mask, out, rows, cols, conn, s);
 }
 
 int recon_f32(Ctx &c, const float *marker, const float *mask, float *out, int rows, int cols, int conn,
               cudaStream_t s) {
-    return run_recon_cta<float, 64, 64, 67>(c, marker, mask, out, rows, cols, conn, s);
+    const int nw = recon_warps();
+    if (nw == 8) return run_recon_cta<float, 64, 64, 67, 8>(c, marker, mask, out, rows, cols, conn, s);
+    if (nw == 32) return run_recon_cta<float, 64, 64, 67, 32>(c, marker, mask, out, rows, cols, conn, s);
+    return run_recon_cta<float, 64, 64, 67, 16>(c, marker, mask, out, rows, cols, conn, s);
 }
 
 }  // namespace nsg

@@ -571,22 +571,26 @@ __global__ void k_bfs_prep(PW a, uint8_t *nbm) {
 // is neither popped nor queued at T_e records the smallest key that touches
 // it: the order in which R pushes it.
 //
-// One thread-block cluster runs the BFS (one CTA per SM, up to 16).  A layer
-// is split into contiguous chunks, one per CTA; after the claims a cluster
+// One thread-block cluster runs the BFS (up to 16 small CTAs, so that other
+// streams' kernels keep the rest of each SM).  A layer is split into
+// contiguous chunks, one per CTA, staged in shared memory; after the claims a cluster
 // barrier, then each CTA compacts its winners in order into its own segment
 // of the next frontier and publishes their count in shared memory; after a
 // second barrier every CTA reads all counts (distributed shared memory) to
 // place the segments.  Chunks are contiguous and ordered by CTA, so the next
 // frontier in global order is the concatenation of the segments.
-constexpr int kBfsThreads = 1024, kBfsItems = 8, kBfsMaxCluster = 16;
+constexpr int kBfsThreads = 256, kBfsCtaItems = 4096, kBfsMaxCluster = 16;
+constexpr int kBfsPerThread = kBfsCtaItems / kBfsThreads;  // <= 16: 64 claim bits per thread
 
-__global__ void __launch_bounds__(kBfsThreads, 1) k_bfs(PW a, const uint8_t *__restrict__ nbm) {
+__global__ void __launch_bounds__(kBfsThreads) k_bfs(PW a, const uint8_t *__restrict__ nbm) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
     const int C = (int)cl.num_blocks(), me = (int)cl.block_rank();
     __shared__ int sh[40];
     __shared__ int tot;                      // winners of this CTA in the last layer
     __shared__ int offs[kBfsMaxCluster + 1];  // where each CTA's segment starts in global order
+    __shared__ int s_r[kBfsCtaItems];         // this CTA's chunk of the frontier
+    __shared__ uint8_t s_m[kBfsCtaItems];     // and the chunk's neighbour classes
     const bool on = a.ctl[W_EVENT] && !a.ctl[W_FALLBACK];
     const int W = a.W;
     int *Fc = a.fr0, *Fn = a.fr1;
@@ -615,51 +619,48 @@ __global__ void __launch_bounds__(kBfsThreads, 1) k_bfs(PW a, const uint8_t *__r
         if (s == 0) break;
         const int per_cta = (s + C - 1) / C;
         const int segcap = 4 * per_cta;
-        if (per_cta > kBfsThreads * kBfsItems || (int64_t)segcap * C > (int64_t)a.n) {
+        if (per_cta > kBfsCtaItems || (int64_t)segcap * C > (int64_t)a.n) {
             if (me == 0 && threadIdx.x == 0) set_fallback(a, 9);  // frontier too wide: serial flood
             break;
         }
-        const int lo = min(s, me * per_cta), hi = min(s, lo + per_cta);
-        const int pt = (hi - lo + kBfsThreads - 1) / kBfsThreads;
-        const int i0 = lo + threadIdx.x * pt;
-        int rr[kBfsItems];
-        uint8_t mm[kBfsItems];
+        const int lo = min(s, me * per_cta), hi = min(s, lo + per_cta), cnt = hi - lo;
+        // stage the chunk (the frontier is read in order: coalesced)
         int seg = 0;
-#pragma unroll
-        for (int j = 0; j < kBfsItems; ++j) {
-            const int i = i0 + j;
-            rr[j] = -1;
-            mm[j] = 0;
-            if (j < pt && i < hi) {
-                while (i >= offs[seg + 1]) ++seg;
-                rr[j] = __ldcg(Fc + seg * prevcap + (i - offs[seg]));
-                mm[j] = nbm[rr[j]];
-            }
+        for (int i = lo + threadIdx.x; i < hi; i += kBfsThreads) {
+            while (i >= offs[seg + 1]) ++seg;
+            const int r = __ldcg(Fc + seg * prevcap + (i - offs[seg]));
+            s_r[i - lo] = r;
+            s_m[i - lo] = nbm[r];
         }
-#pragma unroll
-        for (int j = 0; j < kBfsItems; ++j) {
-            const int key0 = (base + i0 + j) * 4;
+        __syncthreads();
+        const int pt = (cnt + kBfsThreads - 1) / kBfsThreads;
+        const int j0 = threadIdx.x * pt;
+        for (int j = 0; j < pt && j0 + j < cnt; ++j) {
+            const int r = s_r[j0 + j];
+            const unsigned m = s_m[j0 + j];
+            const int key0 = (base + lo + j0 + j) * 4;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                if (mm[j] & (1u << k)) atomicMin(a.claim + rr[j] + off[k], key0 + k);
-                if (mm[j] & (16u << k)) atomicMin(a.inj + rr[j] + off[k], key0 + k);
+                if (m & (1u << k)) atomicMin(a.claim + r + off[k], key0 + k);
+                if (m & (16u << k)) atomicMin(a.inj + r + off[k], key0 + k);
             }
         }
         cl.sync();
-        unsigned win = 0;
-#pragma unroll
-        for (int j = 0; j < kBfsItems; ++j) {
-            const int key0 = (base + i0 + j) * 4;
+        unsigned long long win = 0;
+        for (int j = 0; j < pt && j0 + j < cnt; ++j) {
+            const int r = s_r[j0 + j];
+            const unsigned m = s_m[j0 + j];
+            const int key0 = (base + lo + j0 + j) * 4;
 #pragma unroll
             for (int k = 0; k < 4; ++k)
-                if ((mm[j] & (1u << k)) && __ldcg(a.claim + rr[j] + off[k]) == key0 + k) win |= 1u << (j * 4 + k);
+                if ((m & (1u << k)) && __ldcg(a.claim + r + off[k]) == key0 + k) win |= 1ull << (j * 4 + k);
         }
         int total;
-        int pos = cta_exclusive_scan(__popc(win), sh, total);
+        int pos = cta_exclusive_scan(__popcll(win), sh, total);
         while (win) {
-            const int b = __ffs(win) - 1;
+            const int b = __ffsll((long long)win) - 1;
             win &= win - 1;
-            const int q = rr[b >> 2] + off[b & 3];
+            const int q = s_r[j0 + (b >> 2)] + off[b & 3];
             Fn[me * segcap + pos] = q;
             a.st[q] |= S_R;
             ++pos;
