@@ -5,8 +5,13 @@ Workload: the batched-tile configuration — 256 synthetic H&E tiles of uneven
 size (squares 512-4096 px plus ragged slide-edge tiles 4096 x r / r x 4096),
 generated on the device from fixed seeds (nscale_gb300/synth_torch.py; the
 reference's validation slides are not available).  One step = the full
-segmentNuclei pipeline over every tile of the batch through libnsg.so, inputs
-resident in HBM.  Inputs (1.9 Gpixel, 5.6 GB) are far larger than L2.
+segmentNuclei pipeline over every tile of the batch through libnsg.so's
+batched entry point (nsg_segment_nuclei_batch: a pool of workers, each with
+its own context and stream, keeps several tiles in flight), inputs resident in
+HBM.  Inputs (1.9 Gpixel, 5.6 GB) are far larger than L2.  Also reported: the
+same tiles through plain per-tile calls on one stream (the batched speed-up),
+per-stage times, the host-buffer end-to-end rate, and p50/p99 latency of a
+short Poisson-arrival run through the in-process server (nsg_server_*).
 
 Prints ONE JSON line (rank 0).  `--impl reference` times the reference's CPU
 segmentNuclei path instead: the CPU oracle (a restatement of the reference;
@@ -25,19 +30,20 @@ import os
 import statistics
 import subprocess
 import sys
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "segmentNuclei Mpixel/s on 1 GB300, batched vs per-tile; p50/p99 tile latency"
-# algorithmic bytes per pixel of each pipeline stage (read each input once,
-# write each output once at native width; pointwise work fused)
-STAGE_BYTES = {"background": 7, "RBC": 4, "open19": 4, "reconToNuclei": 6, "fillHoles1": 2,
-               "areaThreshold1": 14, "blobsGt45": 4, "fillHoles2": 2, "openBlobs": 4, "30To1000": 14,
-               "dilate": 2, "distTransform": 5, "imhmin": 8, "watershed": 40, "20To1000": 14,
-               "fillHolesLast": 2, "bwlabel2": 5, "bounding_box": 4, "other": 0}
+# algorithmic bytes per pixel of a tile that runs to SUCCESS: each spatial
+# stage reads its inputs once and writes its outputs once at native width,
+# pointwise work fused (front 7, RBC 4, open19 4, recon 6, fill 2, area-open
+# 14, bwselect 4, fill 2, open 4, area-open 14, dilate 2, EDT 5, imhmin 8,
+# minima 17, bwlabel 5, watershed 12, border+mask 6, area-open 14, fill 2,
+# bwlabel 5)
+ALG_BYTES_PER_PX = 137
+
 
 
 def parse():
@@ -48,7 +54,10 @@ def parse():
     ap.add_argument("--impl", default="nsg", choices=["nsg", "reference"])
     ap.add_argument("--tiles", type=int, default=256)
     ap.add_argument("--streams", type=int, default=8,
-                    help="tiles in flight: host threads, each with its own context and CUDA stream")
+                    help="tiles in flight: pool workers, each with its own context and CUDA stream")
+    ap.add_argument("--per-tile-tiles", type=int, default=64, help="tiles timed in the per-tile comparison")
+    ap.add_argument("--serve-tiles", type=int, default=96, help="tiles sent through the server (0 = skip)")
+    ap.add_argument("--serve-load", type=float, default=0.7, help="offered load, fraction of batched throughput")
     ap.add_argument("--cpu-sample-tiles", type=int, default=0, help="tiles in the CPU baseline sample (0 = cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -202,6 +211,7 @@ def run_nsg(args, rank, world, local):
     import torch
     from nscale_gb300 import _lib
     from nscale_gb300.context import Context, ptr
+    from nscale_gb300.serving import TilePool, TileServer
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     L = _lib.load()
@@ -210,108 +220,45 @@ def run_nsg(args, rank, world, local):
     maxc = max(t.shape[1] for t in tiles)
     px = sum(t.shape[0] * t.shape[1] for t in tiles)
     params = _lib.SegParams()
-    statuses = {}
-    tile_ms = []
-
-    class Worker:
-        """One tile in flight: a context (workspace arena), a stream, label buffers."""
-
-        def __init__(self):
-            self.ctx = Context(maxr, maxc, local)
-            self.stream = torch.cuda.Stream(device=dev)
-            self.sh = C.c_void_p(self.stream.cuda_stream)
-            self.labels = torch.empty(maxr * maxc, dtype=torch.int32, device=dev)
-            self.host_lab = None
-            self.cc = C.c_int(0)
-
-    workers = [Worker() for _ in range(max(1, args.streams))]
-
-    def run_tiles(fn, items, pool):
-        """Hand `items` to the workers of `pool` (one host thread each) until all are done."""
-        nxt = [0]
-        lock = threading.Lock()
-        errors = []
-
-        def loop(w):
-            try:
-                with torch.cuda.stream(w.stream):
-                    while True:
-                        with lock:
-                            i = nxt[0]
-                            nxt[0] += 1
-                        if i >= len(items):
-                            return
-                        fn(w, items[i])
-            except Exception as e:  # noqa: BLE001 - re-raised on the main thread
-                errors.append(e)
-
-        ths = [threading.Thread(target=loop, args=(w,)) for w in pool]
-        for th in ths:
-            th.start()
-        for th in ths:
-            th.join()
-        if errors:
-            raise errors[0]
-
-    def seg_device(w, t, record_latency=False):
-        r, c = t.shape[0], t.shape[1]
-        t0 = time.perf_counter()
-        st = L.nsg_segment_nuclei(w.ctx.h, ptr(t), r, c, c * 3, C.byref(params), ptr(w.labels), None,
-                                  C.byref(w.cc), None, w.sh)
-        if st < 0:
-            raise _lib.NsgError(st, w.ctx.last_error())
-        if record_latency:
-            w.stream.synchronize()
-            tile_ms.append((time.perf_counter() - t0) * 1e3)
-            statuses[st] = statuses.get(st, 0) + 1
+    main = torch.cuda.current_stream(dev)
 
     def barrier():
         if world > 1:
             import torch.distributed as dist
             dist.barrier()
 
-    main = torch.cuda.current_stream(dev)
-
-    def timed(fn, items, n_steps):
-        """CUDA-event time of n_steps passes over `items` on all workers."""
+    def event_time(fn):
+        """CUDA-event time (ms) of a blocking host call: events on the main
+        stream bracket the call, with the device synchronised on both sides."""
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         ev0.record(main)
-        for w in workers:
-            w.stream.wait_event(ev0)
-        for _ in range(n_steps):
-            run_tiles(fn, items, workers)
-        for w in workers:
-            main.wait_stream(w.stream)
+        main.synchronize()
+        fn()
         ev1.record(main)
         torch.cuda.synchronize()
         return ev0.elapsed_time(ev1)
 
+    # ---- batched form: every tile of the batch on the pool's workers --------
+    pool = TilePool(maxr, maxc, workers=max(1, args.streams), device=local)
+    labels = [torch.empty(t.shape[0] * t.shape[1], dtype=torch.int32, device=dev) for t in tiles]
+    arr = (_lib.Tile * len(tiles))()
+    for i, t in enumerate(tiles):
+        arr[i].bgr, arr[i].rows, arr[i].cols, arr[i].row_stride_bytes = t.data_ptr(), t.shape[0], t.shape[1], 0
+        arr[i].labels, arr[i].mask, arr[i].want_bbox = labels[i].data_ptr(), None, 0
     for _ in range(args.warmup):
-        run_tiles(seg_device, tiles, workers)
-    torch.cuda.synchronize()
-    for w in workers:
-        L.nsg_context_set_timing(w.ctx.h, 1)
+        pool.run(arr, params)
     barrier()
     launches0 = L.nsg_kernel_launches()
     with Clocks(local) as clk:
-        total_ms = timed(seg_device, tiles, args.steps)
+        total_ms = event_time(lambda: [pool.run(arr, params) for _ in range(args.steps)])
     launches = L.nsg_kernel_launches() - launches0
     barrier()
-    stage_ms = [0.0] * 19
-    for w in workers:
-        sm = (C.c_double * 19)()
-        calls = C.c_longlong(0)
-        L.nsg_context_stage_times(w.ctx.h, sm, 19, C.byref(calls))
-        L.nsg_context_set_timing(w.ctx.h, 0)
-        for i in range(19):
-            stage_ms[i] += sm[i]
-    names = [L.nsg_stage_name(i).decode() for i in range(19)]
-    # per-tile latency: one tile at a time on one worker (separate pass)
-    run_tiles(lambda w, t: seg_device(w, t, record_latency=True), tiles, workers[:1])
+    statuses = {}
+    for i in range(len(tiles)):
+        statuses[arr[i].status] = statuses.get(arr[i].status, 0) + 1
     ms_step = total_ms / args.steps
-    value_rank = px / (ms_step / 1e3) / 1e6
     if world > 1:
         import torch.distributed as dist
         tmax = torch.tensor([ms_step], dtype=torch.float64)
@@ -319,37 +266,69 @@ def run_nsg(args, rank, world, local):
         ms_step = float(tmax.item())
     value = world * px / (ms_step / 1e3) / 1e6
 
-    # roofline: the stage with the most device time in the timed region
-    per_stage = {names[i]: stage_ms[i] for i in range(19)}
-    dom = max(per_stage, key=per_stage.get)
-    dom_ms_per_step = per_stage[dom] / args.steps
-    dom_bytes = STAGE_BYTES[dom] * px
-    peak, peak_kind = peaks()
-    achieved = dom_bytes / (dom_ms_per_step / 1e3) / 1e9 if dom_ms_per_step > 0 else 0.0
-
-    # e2e: host (pinned) tiles through the public host entry point, labels read
-    # back to pinned host memory; copies both ways inside the timed region
+    # ---- e2e: host (pinned) tiles in, labels back to pinned host memory,
+    # through the same batched entry point; copies inside the timed region
     e2e_tiles = tiles[: min(len(tiles), 64)]
     host_in = [t.cpu().pin_memory() for t in e2e_tiles]
-    for w in workers:
-        w.host_lab = torch.empty(maxr * maxc, dtype=torch.int32).pin_memory()
+    host_lab = [torch.empty(t.shape[0] * t.shape[1], dtype=torch.int32).pin_memory() for t in e2e_tiles]
+    harr = (_lib.Tile * len(host_in))()
+    for i, h in enumerate(host_in):
+        harr[i].bgr, harr[i].rows, harr[i].cols, harr[i].row_stride_bytes = h.data_ptr(), h.shape[0], h.shape[1], 0
+        harr[i].labels, harr[i].mask, harr[i].want_bbox = host_lab[i].data_ptr(), None, 0
     e2e_px = sum(t.shape[0] * t.shape[1] for t in e2e_tiles)
+    pool.run(harr, params, host=True)
+    e2e_ms = event_time(lambda: [pool.run(harr, params, host=True) for _ in range(args.steps)]) / args.steps
+    e2e_value = world * e2e_px / (e2e_ms / 1e3) / 1e6
+    pool.close()
 
-    def seg_host(w, h):
-        r, c = h.shape[0], h.shape[1]
-        st = L.nsg_segment_nuclei_host(w.ctx.h, C.c_void_p(h.data_ptr()), r, c, C.byref(params),
-                                       C.c_void_p(w.host_lab.data_ptr()), None, C.byref(w.cc), None, w.sh)
-        if st < 0:
-            raise _lib.NsgError(st, w.ctx.last_error())
+    # ---- per-tile form: the same tiles one call at a time on one stream,
+    # with per-stage CUDA-event timing (the stage table below)
+    n_pt = min(len(tiles), args.per_tile_tiles)
+    pt_tiles = tiles[:n_pt]
+    pt_px = sum(t.shape[0] * t.shape[1] for t in pt_tiles)
+    ctx = Context(maxr, maxc, local)
+    stream = torch.cuda.Stream(device=dev)
+    sh = C.c_void_p(stream.cuda_stream)
+    lab1 = torch.empty(maxr * maxc, dtype=torch.int32, device=dev)
+    cc = C.c_int(0)
+    tile_ms = []
 
-    run_tiles(seg_host, host_in, workers)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        run_tiles(seg_host, host_in, workers)
-    torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    e2e_value = world * e2e_px / e2e_s / 1e6
+    def per_tile(record=False):
+        for t in pt_tiles:
+            t0 = time.perf_counter()
+            st = L.nsg_segment_nuclei(ctx.h, ptr(t), t.shape[0], t.shape[1], t.shape[1] * 3, C.byref(params),
+                                      ptr(lab1), None, C.byref(cc), None, sh)
+            if st < 0:
+                raise _lib.NsgError(st, ctx.last_error())
+            if record:
+                stream.synchronize()
+                tile_ms.append((time.perf_counter() - t0) * 1e3)
+
+    with torch.cuda.stream(stream):
+        per_tile()
+        L.nsg_context_set_timing(ctx.h, 1)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        per_tile()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        pt_ms = ev0.elapsed_time(ev1)
+        stage_ms = (C.c_double * 19)()
+        calls = C.c_longlong(0)
+        L.nsg_context_stage_times(ctx.h, stage_ms, 19, C.byref(calls))
+        L.nsg_context_set_timing(ctx.h, 0)
+        per_tile(record=True)  # latency of one tile alone
+    names = [L.nsg_stage_name(i).decode() for i in range(19)]
+    per_stage = {names[i]: stage_ms[i] for i in range(19)}
+    pt_value = pt_px / (pt_ms / 1e3) / 1e6
+    ctx.close()
+
+    # ---- serving: Poisson arrivals of host tiles into the server ------------
+    serving = None
+    if rank == 0 and args.serve_tiles > 0:
+        serving = serve(args, tiles, value / world)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -364,8 +343,9 @@ def run_nsg(args, rank, world, local):
 
     if rank != 0:
         return
+    peak, peak_kind = peaks()
+    achieved = value * ALG_BYTES_PER_PX / 1e3  # Mpixel/s x B/px -> GB/s
     lat = sorted(tile_ms)
-    clk = clk.summary()
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mpixel/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
@@ -373,23 +353,73 @@ def run_nsg(args, rank, world, local):
         "config": {"workload": f"segmentNuclei over {len(tiles)} uneven synthetic H&E tiles "
                                f"(squares 512-4096 + ragged edge tiles), device-resident inputs",
                    "tiles": len(tiles), "pixels_per_step": px,
-                   "form": f"per-tile calls, {len(workers)} tiles in flight (host threads, one context and "
-                           f"stream each)",
+                   "form": f"batched: nsg_segment_nuclei_batch, {pool_workers(args)} tiles in flight "
+                           f"(one context and stream per worker)",
                    "l2": "inputs larger than L2 (5.6 GB per step)", "parallelism": f"replicas x{world}"},
-        "latency_ms": {"p50": round(lat[len(lat) // 2], 3), "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3)},
+        "per_tile": {"value": round(pt_value, 3), "unit": "Mpixel/s", "tiles": n_pt,
+                     "form": "nsg_segment_nuclei one tile at a time on one stream",
+                     "batched_speedup": round(value / world / pt_value, 2)},
+        "latency_ms": {"p50": round(lat[len(lat) // 2], 3),
+                       "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3),
+                       "what": "one tile alone, per-tile form"},
         "statuses": {str(k): v for k, v in statuses.items()},
-        "stage_ms_per_step": {k: round(v / args.steps, 3) for k, v in per_stage.items() if v > 0},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+        "stage_ms_per_tile_pass": {k: round(v, 3) for k, v in per_stage.items() if v > 0},
+        "roofline": {"bound": "hbm", "kernel": "segmentNuclei pipeline, all stages (batched)",
+                     "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 5), "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_launch": dom_bytes, "traffic": None},
+                     "algorithmic_bytes_per_px": ALG_BYTES_PER_PX, "traffic": None},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mpixel/s", "h2d_bytes_per_step": int(3 * e2e_px),
                 "d2h_bytes_per_step": int(4 * e2e_px), "tiles": len(e2e_tiles)},
         "gpu_launches": int(launches),
-        "clocks": clk,
+        "clocks": clk.summary(),
     }
+    if serving:
+        line["serving"] = serving
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
+
+
+def pool_workers(args):
+    return max(1, args.streams)
+
+
+def serve(args, tiles, batched_mpx_s):
+    """Poisson arrivals of host tiles into nsg_server at `serve_load` x the
+    batched throughput; returns latency percentiles (submit -> result)."""
+    import numpy as np
+    import random
+    from nscale_gb300 import _lib
+    from nscale_gb300.serving import TileServer
+    sub = tiles[: args.serve_tiles]
+    host = [t.cpu().numpy() for t in sub]
+    labs = [np.empty(h.shape[:2], np.int32) for h in host]
+    maxr = max(h.shape[0] for h in host)
+    maxc = max(h.shape[1] for h in host)
+    per = _lib.load().nsg_pool_context_bytes(maxr, maxc)
+    srv = TileServer(maxr, maxc, memory_budget_bytes=per * max(1, args.streams), queue_cap=len(host))
+    mean_px = sum(h.shape[0] * h.shape[1] for h in host) / len(host)
+    rate = args.serve_load * batched_mpx_s * 1e6 / mean_px  # tiles per second
+    rng = random.Random(0x5EED0004)
+    results = []
+    t0 = time.perf_counter()
+    due = t0
+    for h, lab in zip(host, labs):
+        due += rng.expovariate(rate)
+        while time.perf_counter() < due:
+            results += srv.poll(64, 0)
+            time.sleep(min(0.0005, max(0.0, due - time.perf_counter())))
+        srv.submit(h, lab)
+    while len(results) < len(host):
+        results += srv.poll(64, 100)
+    wall = time.perf_counter() - t0
+    workers = srv.workers
+    srv.close()
+    lat = sorted(r["latency_ms"] for r in results)
+    return {"tiles": len(host), "arrivals": "poisson", "offered_tiles_per_s": round(rate, 2),
+            "load": args.serve_load, "workers": workers,
+            "p50_ms": round(lat[len(lat) // 2], 3), "p99_ms": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3),
+            "achieved_tiles_per_s": round(len(host) / wall, 2)}
 
 
 def main():

@@ -173,8 +173,9 @@ int nsg_watershed_serial(nsg_context *ctx, const uint8_t *bgr, const float *img,
  * [0] fallback code (0 = domain-parallel path taken), [1] flood domains,
  * [2] background entries recorded, [6] level of the first background pop,
  * [9] 1 if a background flood event happened, [11] BFS layers; and of the
- * last grey reconstruction: [12] tile passes, [13] row+column sweeps;
- * [14] CTAs in the BFS cluster. */
+ * last grey reconstruction: [12] tile passes, [13] in-tile row+column
+ * sweeps, [15] pixels changed by its whole-image sweeps; [14] CTAs in the
+ * BFS cluster. */
 int nsg_watershed_diagnostics(nsg_context *ctx, int *out16, nsg_stream_t stream);
 /* ConnComponents::boundingBox (ConnComponents.cpp:241-284) on a -1-background
  * label image: writes compcount entries of (label, minx, maxx, miny, maxy) as
@@ -203,6 +204,61 @@ int nsg_segment_nuclei(nsg_context *ctx, const uint8_t *bgr, int rows, int cols,
 int nsg_segment_nuclei_host(nsg_context *ctx, const uint8_t *bgr_host, int rows, int cols, const nsg_seg_params *p,
                             int32_t *labels_host, uint8_t *mask_host, int *compcount, int32_t **bbox,
                             nsg_stream_t stream);
+
+/* ---- many tiles: the batched form and the in-process server ---------------- */
+/* The reference farms tiles to processes, one segmentNuclei call each
+ * (nu-segment.cpp:274-430, one tile per MPI rank at a time).  Here one
+ * process keeps several tiles in flight on one GPU: a pool of workers, each a
+ * host thread with its own context (workspace arena) and CUDA stream, so that
+ * the latency-bound stages of one tile overlap the others. */
+typedef struct nsg_tile {
+    const uint8_t *bgr;      /* BGR interleaved uint8 (device, or host with NSG_TILE_HOST) */
+    int rows, cols;
+    size_t row_stride_bytes; /* device tiles only; 0 = 3 * cols (host tiles are dense) */
+    int32_t *labels;         /* nullable output (same memory kind as bgr) */
+    uint8_t *mask;           /* nullable output (same memory kind as bgr) */
+    int want_bbox;           /* 1: fill bbox (nsg_alloc'd, free with nsg_free) */
+    /* results */
+    int status;              /* segmentNuclei status or NSG_ERR_* */
+    int compcount;
+    int32_t *bbox;
+} nsg_tile;
+#define NSG_TILE_HOST 1 /* flag: bgr / labels / mask are host pointers */
+
+typedef struct nsg_pool nsg_pool;
+/* `workers` tiles in flight (contexts sized for max_rows x max_cols). */
+int nsg_pool_create(nsg_pool **pool, int max_rows, int max_cols, int workers, int device);
+int nsg_pool_destroy(nsg_pool *pool);
+int nsg_pool_workers(const nsg_pool *pool);
+/* segmentNuclei on every tile of `tiles` (any order, all workers); returns
+ * when all are done.  Per-tile statuses land in tiles[i].status; the return
+ * value is NSG_SUCCESS or the first NSG_ERR_* a tile produced.  p NULL =
+ * defaults (HistologicalEntities.h:52-54). */
+int nsg_segment_nuclei_batch(nsg_pool *pool, nsg_tile *tiles, int n, const nsg_seg_params *p, int flags);
+
+/* In-process server (serving form): tiles are submitted one at a time (host
+ * memory), processed FIFO by the pool's workers, and collected with poll.
+ * The number of workers is what the memory budget admits (one context of
+ * nsg_pool_context_bytes each); submit returns NSG_ERR_QUEUE_FULL while
+ * `queue_cap` tiles are waiting.  The caller keeps a submitted tile's buffers
+ * alive until its result has been polled. */
+typedef struct nsg_server nsg_server;
+typedef struct nsg_result {
+    long long ticket;
+    int status, compcount;
+    int32_t *bbox;           /* when the tile asked for it: nsg_alloc'd, free with nsg_free */
+    double latency_ms;       /* submit -> result ready */
+} nsg_result;
+size_t nsg_pool_context_bytes(int max_rows, int max_cols);
+int nsg_server_create(nsg_server **srv, int max_rows, int max_cols, size_t memory_budget_bytes, int queue_cap,
+                      int device);
+int nsg_server_workers(const nsg_server *srv);
+/* `tile` is copied (its pointers are not); *ticket identifies the result */
+int nsg_server_submit(nsg_server *srv, const nsg_tile *tile, const nsg_seg_params *p, long long *ticket);
+/* up to max finished results, waiting up to wait_ms for the first; returns
+ * how many were written */
+int nsg_server_poll(nsg_server *srv, nsg_result *out, int max, int wait_ms);
+int nsg_server_destroy(nsg_server *srv);
 
 /* Per-stage CUDA-event timing of segmentNuclei, in place of the reference's
  * SimpleCSVLogger::logTimeSinceLastLog (UtilsLogger.h:85-183; stage names as

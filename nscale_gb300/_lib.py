@@ -43,6 +43,23 @@ class SegParams(C.Structure):
             setattr(self, k, v)
 
 
+class Tile(C.Structure):
+    """nsg_tile: one tile of a batch or server submission (include/nsg.h)."""
+
+    _fields_ = [("bgr", C.c_void_p), ("rows", C.c_int), ("cols", C.c_int), ("row_stride_bytes", C.c_size_t),
+                ("labels", C.c_void_p), ("mask", C.c_void_p), ("want_bbox", C.c_int),
+                ("status", C.c_int), ("compcount", C.c_int), ("bbox", C.POINTER(C.c_int32))]
+
+
+class Result(C.Structure):
+    """nsg_result: one finished server tile."""
+
+    _fields_ = [("ticket", C.c_longlong), ("status", C.c_int), ("compcount", C.c_int),
+                ("bbox", C.POINTER(C.c_int32)), ("latency_ms", C.c_double)]
+
+
+TILE_HOST = 1
+
 _P = C.c_void_p
 _I = C.c_int
 _SIGS = {
@@ -65,6 +82,16 @@ _SIGS = {
     "nsg_imreconstruct_binary_u8": (_I, [_P, _P, _P, _P, _I, _I, _I, _P]),
     "nsg_imfill_holes_u8": (_I, [_P, _P, _P, _I, _I, _I, _P]),
     "nsg_imfill_holes_u8_noalloc": (_I, [_P, _P, _I, _I, _I, _P]),
+    "nsg_pool_create": (_I, [C.POINTER(_P), _I, _I, _I, _I]),
+    "nsg_pool_destroy": (_I, [_P]),
+    "nsg_pool_workers": (_I, [_P]),
+    "nsg_pool_context_bytes": (C.c_size_t, [_I, _I]),
+    "nsg_segment_nuclei_batch": (_I, [_P, C.POINTER(Tile), _I, C.POINTER(SegParams), _I]),
+    "nsg_server_create": (_I, [C.POINTER(_P), _I, _I, C.c_size_t, _I, _I]),
+    "nsg_server_workers": (_I, [_P]),
+    "nsg_server_submit": (_I, [_P, C.POINTER(Tile), C.POINTER(SegParams), C.POINTER(C.c_longlong)]),
+    "nsg_server_poll": (_I, [_P, C.POINTER(Result), _I, _I]),
+    "nsg_server_destroy": (_I, [_P]),
     "nsg_bwselect_u8": (_I, [_P, _P, _P, _P, _I, _I, _I, _P]),
     "nsg_bwlabel": (_I, [_P, _P, _P, _I, _I, _I, _P]),
     "nsg_bwareaopen": (_I, [_P, _P, _P, _I, _I, _I, _I, _I, C.POINTER(_I), _P]),

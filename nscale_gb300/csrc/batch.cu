@@ -1,0 +1,273 @@
+// batch.cu — many tiles on one GPU: a pool of workers (host threads), each
+// owning a context (workspace arena) and a non-blocking CUDA stream.
+//
+// The reference segments one tile per process and farms tiles to MPI ranks
+// (nu-segment.cpp:274-430).  On one GB300 a single tile leaves most SMs idle
+// during its latency-bound stages (the watershed's layer-by-layer BFS and
+// per-domain floods, the tail of the reconstruction queue), so the pool keeps
+// several tiles in flight and lets their stages overlap:
+//
+//  * nsg_segment_nuclei_batch: every worker takes the next tile index from a
+//    shared counter until the batch is done (largest-first order is the
+//    caller's choice);
+//  * nsg_server_*: tiles are submitted one at a time into a bounded FIFO and
+//    results are polled; the number of workers is what a memory budget admits.
+//
+// Host code only: the device work is the pipeline of pipeline.cu.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "nsg_internal.cuh"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Job {
+    nsg_tile tile;
+    nsg_seg_params prm;
+    long long ticket;
+    Clock::time_point t_submit;
+};
+
+struct Worker {
+    nsg_context *ctx = nullptr;
+    cudaStream_t stream = nullptr;
+    std::thread th;
+};
+
+// one tile through the pipeline on a worker; outputs are complete on return
+void run_tile(nsg_context *ctx, cudaStream_t s, nsg_tile &t, const nsg_seg_params &p, bool host) {
+    t.compcount = 0;
+    t.bbox = nullptr;
+    int32_t **bb = t.want_bbox ? &t.bbox : nullptr;
+    int st;
+    if (host) {
+        st = nsg_segment_nuclei_host(ctx, t.bgr, t.rows, t.cols, &p, t.labels, t.mask, &t.compcount, bb, s);
+    } else {
+        const size_t stride = t.row_stride_bytes ? t.row_stride_bytes : (size_t)t.cols * 3;
+        st = nsg_segment_nuclei(ctx, t.bgr, t.rows, t.cols, stride, &p, t.labels, t.mask, &t.compcount, bb, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess && st >= 0) st = NSG_ERR_CUDA;
+    }
+    t.status = st;
+}
+
+}  // namespace
+
+struct nsg_pool {
+    int device = 0;
+    std::vector<Worker> w;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done, cv_res;
+    bool quit = false;
+    // batch job (published under mu, then read lock-free by the workers)
+    nsg_tile *tiles = nullptr;
+    int n = 0;
+    nsg_seg_params prm{};
+    int flags = 0;
+    std::atomic<int> next{0};
+    std::atomic<int> first_error{0};
+    unsigned long long gen = 0;
+    int busy = 0;
+    // server queue
+    std::deque<Job> q;
+    std::deque<nsg_result> done;
+    int qcap = 0;
+    long long next_ticket = 0;
+
+    void work(int k) {
+        cudaSetDevice(device);
+        Worker &me = w[k];
+        unsigned long long seen = 0;
+        for (;;) {
+            std::unique_lock<std::mutex> lk(mu);
+            cv_work.wait(lk, [&] { return quit || gen != seen || !q.empty(); });
+            if (quit) return;
+            if (gen == seen && !q.empty()) {
+                Job j = q.front();
+                q.pop_front();
+                lk.unlock();
+                run_tile(me.ctx, me.stream, j.tile, j.prm, true);
+                nsg_result r;
+                r.ticket = j.ticket;
+                r.status = j.tile.status;
+                r.compcount = j.tile.compcount;
+                r.bbox = j.tile.bbox;
+                r.latency_ms = std::chrono::duration<double, std::milli>(Clock::now() - j.t_submit).count();
+                lk.lock();
+                done.push_back(r);
+                cv_res.notify_all();
+                continue;
+            }
+            seen = gen;
+            lk.unlock();
+            const bool host = flags & NSG_TILE_HOST;
+            for (;;) {
+                const int i = next.fetch_add(1);
+                if (i >= n) break;
+                run_tile(me.ctx, me.stream, tiles[i], prm, host);
+                if (tiles[i].status < NSG_RUNTIME_FAILED) {
+                    int zero = 0;
+                    first_error.compare_exchange_strong(zero, tiles[i].status);
+                }
+            }
+            lk.lock();
+            if (--busy == 0) cv_done.notify_all();
+        }
+    }
+};
+
+struct nsg_server {
+    nsg_pool *pool = nullptr;
+};
+
+namespace {
+
+void pool_free(nsg_pool *p) {
+    {
+        std::lock_guard<std::mutex> lk(p->mu);
+        p->quit = true;
+    }
+    p->cv_work.notify_all();
+    for (auto &w : p->w)
+        if (w.th.joinable()) w.th.join();
+    cudaSetDevice(p->device);
+    for (auto &w : p->w) {
+        if (w.stream) cudaStreamDestroy(w.stream);
+        if (w.ctx) nsg_context_destroy(w.ctx);
+    }
+    delete p;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t nsg_pool_context_bytes(int max_rows, int max_cols) {
+    if (max_rows <= 0 || max_cols <= 0) return 0;
+    return nsg::context_bytes_for(max_rows, max_cols);
+}
+
+int nsg_pool_create(nsg_pool **out, int max_rows, int max_cols, int workers, int device) {
+    if (!out || max_rows <= 0 || max_cols <= 0 || workers <= 0 || workers > 256) return NSG_ERR_ARG;
+    *out = nullptr;
+    nsg_pool *p = new (std::nothrow) nsg_pool();
+    if (!p) return NSG_ERR_OOM;
+    p->device = device;
+    p->w.resize(workers);
+    if (cudaSetDevice(device) != cudaSuccess) {
+        delete p;
+        return NSG_ERR_CUDA;
+    }
+    for (auto &w : p->w) {
+        int r = nsg_context_create(&w.ctx, max_rows, max_cols, device);
+        if (r == NSG_SUCCESS && cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking) != cudaSuccess)
+            r = NSG_ERR_CUDA;
+        if (r != NSG_SUCCESS) {
+            pool_free(p);
+            return r;
+        }
+    }
+    for (int k = 0; k < workers; ++k) p->w[k].th = std::thread([p, k] { p->work(k); });
+    *out = p;
+    return NSG_SUCCESS;
+}
+
+int nsg_pool_destroy(nsg_pool *p) {
+    if (!p) return NSG_ERR_ARG;
+    pool_free(p);
+    return NSG_SUCCESS;
+}
+
+int nsg_pool_workers(const nsg_pool *p) { return p ? (int)p->w.size() : 0; }
+
+int nsg_segment_nuclei_batch(nsg_pool *p, nsg_tile *tiles, int n, const nsg_seg_params *prm, int flags) {
+    if (!p || n < 0 || (n > 0 && !tiles)) return NSG_ERR_ARG;
+    if (n == 0) return NSG_SUCCESS;
+    std::unique_lock<std::mutex> lk(p->mu);
+    if (p->busy) return NSG_ERR_ARG;  // one batch at a time per pool
+    p->tiles = tiles;
+    p->n = n;
+    if (prm) p->prm = *prm;
+    else nsg_default_params(&p->prm);
+    p->flags = flags;
+    p->next.store(0);
+    p->first_error.store(0);
+    p->busy = (int)p->w.size();
+    ++p->gen;
+    p->cv_work.notify_all();
+    p->cv_done.wait(lk, [&] { return p->busy == 0; });
+    const int e = p->first_error.load();
+    return e ? e : NSG_SUCCESS;
+}
+
+int nsg_server_create(nsg_server **out, int max_rows, int max_cols, size_t budget, int queue_cap, int device) {
+    if (!out || queue_cap <= 0) return NSG_ERR_ARG;
+    *out = nullptr;
+    const size_t per = nsg_pool_context_bytes(max_rows, max_cols);
+    if (per == 0) return NSG_ERR_ARG;
+    const size_t admit = budget / per;
+    if (admit < 1) return NSG_ERR_OOM;  // the budget does not hold one tile's workspace
+    const int workers = (int)std::min<size_t>(admit, 64);
+    nsg_server *s = new (std::nothrow) nsg_server();
+    if (!s) return NSG_ERR_OOM;
+    int r = nsg_pool_create(&s->pool, max_rows, max_cols, workers, device);
+    if (r != NSG_SUCCESS) {
+        delete s;
+        return r;
+    }
+    s->pool->qcap = queue_cap;
+    *out = s;
+    return NSG_SUCCESS;
+}
+
+int nsg_server_workers(const nsg_server *s) { return s ? nsg_pool_workers(s->pool) : 0; }
+
+int nsg_server_submit(nsg_server *s, const nsg_tile *tile, const nsg_seg_params *prm, long long *ticket) {
+    if (!s || !tile || !tile->bgr) return NSG_ERR_ARG;
+    nsg_pool *p = s->pool;
+    Job j;
+    j.tile = *tile;
+    if (prm) j.prm = *prm;
+    else nsg_default_params(&j.prm);
+    j.t_submit = Clock::now();
+    {
+        std::lock_guard<std::mutex> lk(p->mu);
+        if ((int)p->q.size() >= p->qcap) return NSG_ERR_QUEUE_FULL;
+        j.ticket = p->next_ticket++;
+        p->q.push_back(j);
+    }
+    if (ticket) *ticket = j.ticket;
+    p->cv_work.notify_one();
+    return NSG_SUCCESS;
+}
+
+int nsg_server_poll(nsg_server *s, nsg_result *out, int max, int wait_ms) {
+    if (!s || !out || max <= 0) return NSG_ERR_ARG;
+    nsg_pool *p = s->pool;
+    std::unique_lock<std::mutex> lk(p->mu);
+    if (p->done.empty() && wait_ms > 0)
+        p->cv_res.wait_for(lk, std::chrono::milliseconds(wait_ms), [&] { return !p->done.empty(); });
+    int k = 0;
+    while (k < max && !p->done.empty()) {
+        out[k++] = p->done.front();
+        p->done.pop_front();
+    }
+    return k;
+}
+
+int nsg_server_destroy(nsg_server *s) {
+    if (!s) return NSG_ERR_ARG;
+    pool_free(s->pool);
+    delete s;
+    return NSG_SUCCESS;
+}
+
+}  // extern "C"

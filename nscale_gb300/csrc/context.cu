@@ -30,6 +30,32 @@ int reset_status(Ctx &c, cudaStream_t s) {
     return NSG_SUCCESS;
 }
 
+// sizes of the arena's slots, in carving order; returns the total
+size_t arena_layout(int64_t max_pad, size_t *sizes) {
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t P = (size_t)max_pad;
+    int ns = 0;
+    for (int i = 0; i < 6; ++i) sizes[ns++] = al(P * 4);
+    for (int i = 0; i < 3; ++i) sizes[ns++] = al(P * 4);
+    for (int i = 0; i < 4; ++i) sizes[ns++] = al(P);
+    for (int i = 0; i < 10; ++i) sizes[ns++] = al(P);
+    for (int i = 0; i < 2; ++i) sizes[ns++] = al(P * 4);
+    for (int i = 0; i < 2; ++i) sizes[ns++] = al(P * 4);
+    sizes[ns++] = al(P * 3);                 // p_bgr
+    sizes[ns++] = al(kCtrlInts * 4);         // ctrl
+    sizes[ns++] = al(64 * 8);                // ctr64
+    sizes[ns++] = al((P / 256 + 1024) * 4);  // scan_tmp
+    sizes[ns++] = al(pws_workspace_bytes((int64_t)P));  // watershed workspace
+    size_t total = 0;
+    for (int i = 0; i < ns; ++i) total += sizes[i];
+    return total;
+}
+
+size_t context_bytes_for(int max_rows, int max_cols) {
+    size_t sizes[64];
+    return arena_layout((int64_t)(max_rows + 2) * (max_cols + 2), sizes);
+}
+
 }  // namespace nsg
 
 using namespace nsg;
@@ -90,23 +116,8 @@ int nsg_context_create(nsg_context **out, int max_rows, int max_cols, int device
         return NSG_ERR_CUDA;
     }
     cudaDeviceGetAttribute(&c.sm_count, cudaDevAttrMultiProcessorCount, device);
-    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const size_t P = (size_t)c.max_pad;
     size_t sizes[64];
-    int ns = 0;
-    for (int i = 0; i < 6; ++i) sizes[ns++] = al(P * 4);
-    for (int i = 0; i < 3; ++i) sizes[ns++] = al(P * 4);
-    for (int i = 0; i < 4; ++i) sizes[ns++] = al(P);
-    for (int i = 0; i < 10; ++i) sizes[ns++] = al(P);
-    for (int i = 0; i < 2; ++i) sizes[ns++] = al(P * 4);
-    for (int i = 0; i < 2; ++i) sizes[ns++] = al(P * 4);
-    sizes[ns++] = al(P * 3);                 // p_bgr
-    sizes[ns++] = al(kCtrlInts * 4);         // ctrl
-    sizes[ns++] = al(64 * 8);                // ctr64
-    sizes[ns++] = al((P / 256 + 1024) * 4);  // scan_tmp
-    sizes[ns++] = al(pws_workspace_bytes((int64_t)P));  // watershed workspace
-    size_t total = 0;
-    for (int i = 0; i < ns; ++i) total += sizes[i];
+    const size_t total = arena_layout(c.max_pad, sizes);
     char *base = nullptr;
     if (cudaMalloc((void **)&base, total) != cudaSuccess) {
         cudaGetLastError();

@@ -62,7 +62,7 @@ enum Ctrl : int {
     C_QPEND = 10,
     C_FLAG0 = 16,
     C_FLAG1 = 17,
-    C_RSTATS = 20,   // grey reconstruction: tile passes, sweeps (2 ints)
+    C_RSTATS = 20,   // grey reconstruction: tile passes, sweeps, pixels changed by whole-image sweeps
     C_WS = 64,       // watershed control block (64 ints)
     C_QSLOTS = 1024, // 3072 ints: generic small arrays
 };
@@ -99,6 +99,13 @@ struct Ctx {
 struct nsg_context {
     nsg::Ctx c;
 };
+
+namespace nsg {
+// device bytes of a context for images up to max_rows x max_cols
+size_t context_bytes_for(int max_rows, int max_cols);
+int segment_nuclei_dev(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int cols, const nsg_seg_params &p,
+                       int32_t *labels_out, uint8_t *mask_out, int *compcount, int32_t **bbox, cudaStream_t s);
+}  // namespace nsg
 
 namespace nsg {
 

@@ -92,7 +92,7 @@ __global__ void init_min_f32(const float *__restrict__ a, const float *__restric
 }
 
 // dirty lines a tile starts a pass with (set by the tiles that notify it)
-enum : int { D_N = 1, D_S = 2, D_W = 4, D_E = 8, D_ALL = 16 };
+enum : int { D_N = 1, D_S = 2, D_W = 4, D_E = 8, D_ALL = 16, D_FRESH = 32 };
 
 __global__ void init_queue(int *state, int *queue, int *dirty, int qcap, int ntiles, int *ctrl) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < qcap; i += gridDim.x * blockDim.x) {
@@ -106,6 +106,152 @@ __global__ void init_queue(int *state, int *queue, int *dirty, int qcap, int nti
         ctrl[C_QHEAD] = 0;
         ctrl[C_QTAIL] = ntiles;
         ctrl[C_QPEND] = ntiles;
+        ctrl[C_RSTATS] = 0;
+        ctrl[C_RSTATS + 1] = 0;
+    }
+}
+
+// ---- whole-image sweeps ------------------------------------------------------
+// One thread per row (per column): the raster scan then the anti-raster scan
+// of the reference, restricted to one line, with the cross-line neighbours read
+// as they are (other threads may be raising them: values only grow, so any
+// value read is a valid lower bound).  Outside the image everything is 0, the
+// reference's padding ring.  A few row + column sweeps settle most of an
+// image with almost no SM time held; the tile queue finishes the rest.
+// plain (L1-cached) loads: a stale value is an older lower bound, still valid
+template <typename T>
+__device__ __forceinline__ T at0(const T *p, int64_t i, bool ok) {
+    return ok ? p[i] : (T)0;
+}
+
+template <typename T>
+__global__ void sweep_rows(const T *__restrict__ mask, T *out, int rows, int cols, int conn8, int *changed) {
+    const int y = blockIdx.x * blockDim.x + threadIdx.x;
+    if (y >= rows) return;
+    T *row = out + (int64_t)y * cols;
+    const T *mrow = mask + (int64_t)y * cols;
+    const bool hu = y > 0, hd = y + 1 < rows;
+    const int64_t U = -(int64_t)cols, D = cols;
+    int nch = 0;
+    T prev = (T)0;
+    for (int x = 0; x < cols; ++x) {
+        const T cur = row[x];
+        T w = smax(cur, smax(at0(row, U + x, hu), at0(row, D + x, hd)));
+        if (conn8) {
+            const bool l = x > 0, r = x + 1 < cols;
+            w = smax(w, smax(smax(at0(row, U + x - 1, hu && l), at0(row, U + x + 1, hu && r)),
+                             smax(at0(row, D + x - 1, hd && l), at0(row, D + x + 1, hd && r))));
+        }
+        const T m = mrow[x];
+        const T v = clampv(prev, smin(w, m), m);
+        if (!(v == cur)) {
+            row[x] = v;
+            ++nch;
+        }
+        prev = v;
+    }
+    T nxt = (T)0;
+    for (int x = cols - 1; x >= 0; --x) {
+        const T f = row[x];
+        const T v = clampv(nxt, f, mrow[x]);
+        if (!(v == f)) {
+            row[x] = v;
+            ++nch;
+        }
+        nxt = v;
+    }
+    if (nch) atomicAdd(changed, nch);
+}
+
+// column sweep; when `tdirty` is given, every tile with a changed pixel is
+// marked for the tile queue (full pass, unconditional edge checks)
+template <typename T>
+__global__ void sweep_cols(const T *__restrict__ mask, T *out, int rows, int cols, int conn8, int *changed,
+                           int *tdirty, int tw, int th, int tiles_x) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= cols) return;
+    const bool hl = x > 0, hr = x + 1 < cols;
+    int nch = 0;
+    int last_tile = -1;
+    T prev = (T)0;
+    for (int y = 0; y < rows; ++y) {
+        const int64_t i = (int64_t)y * cols + x;
+        const T cur = out[i];
+        T w = smax(cur, smax(at0(out, i - 1, hl), at0(out, i + 1, hr)));
+        if (conn8) {
+            const bool u = y > 0, d = y + 1 < rows;
+            w = smax(w, smax(smax(at0(out, i - cols - 1, u && hl), at0(out, i - cols + 1, u && hr)),
+                             smax(at0(out, i + cols - 1, d && hl), at0(out, i + cols + 1, d && hr))));
+        }
+        const T m = mask[i];
+        const T v = clampv(prev, smin(w, m), m);
+        if (!(v == cur)) {
+            out[i] = v;
+            ++nch;
+            if (tdirty) {
+                const int t = (y / th) * tiles_x + x / tw;
+                if (t != last_tile) tdirty[t] = D_ALL | D_FRESH;
+                last_tile = t;
+            }
+        }
+        prev = v;
+    }
+    T nxt = (T)0;
+    for (int y = rows - 1; y >= 0; --y) {
+        const int64_t i = (int64_t)y * cols + x;
+        const T f = out[i];
+        const T v = clampv(nxt, f, mask[i]);
+        if (!(v == f)) {
+            out[i] = v;
+            ++nch;
+            if (tdirty) {
+                const int t = (y / th) * tiles_x + x / tw;
+                if (t != last_tile) tdirty[t] = D_ALL | D_FRESH;
+                last_tile = t;
+            }
+        }
+        nxt = v;
+    }
+    if (nch) atomicAdd(changed, nch);
+}
+
+__global__ void zero_ints(int *p, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = 0;
+}
+
+// the tile queue holds exactly the marked tiles (one block, in tile order)
+__global__ void __launch_bounds__(1024) queue_marked(int *state, int *queue, const int *dirty, int qcap, int ntiles,
+                                                     int *ctrl) {
+    __shared__ int wsum[32];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    for (int i = threadIdx.x; i < qcap; i += blockDim.x) queue[i] = 0;
+    __syncthreads();
+    for (int base = 0; base < ntiles; base += blockDim.x) {
+        const int t = base + threadIdx.x;
+        const bool on = t < ntiles && dirty[t] != 0;
+        if (t < ntiles) state[t] = on ? 1 : 0;
+        const unsigned b = __ballot_sync(0xffffffffu, on);
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (lane == 0) wsum[warp] = __popc(b);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int acc = carry;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+                const int v = wsum[w];
+                wsum[w] = acc;
+                acc += v;
+            }
+            carry = acc;
+        }
+        __syncthreads();
+        if (on) queue[wsum[warp] + __popc(b & ((1u << lane) - 1u))] = t + 1;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        ctrl[C_QHEAD] = 0;
+        ctrl[C_QTAIL] = carry;
+        ctrl[C_QPEND] = carry;
         ctrl[C_RSTATS] = 0;
         ctrl[C_RSTATS + 1] = 0;
     }
@@ -455,11 +601,12 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
     // A neighbour tile needs another pass only if an edge pixel that changed
     // here can raise one of its pixels: new value above that pixel's value
     // (as loaded; it can only have grown since) and that pixel below its mask.
-    if (anych) {
+    const bool fresh = dirty_in & D_FRESH;  // the tile changed before this pass: check every edge pixel
+    if (anych || fresh) {
         const int c8 = conn8 ? 1 : 0;
         for (int x = threadIdx.x; x < TW; x += NW * 32) {
             T v = o[P + x + 1];
-            if (!(v == sm.eN[x]))
+            if (fresh || !(v == sm.eN[x]))
                 for (int d = -c8; d <= c8; ++d) {
                     int h = x + d;
                     if (h < 0 || h >= TW) continue;
@@ -467,7 +614,7 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
                     if (v > hv && sm.mN[h + 1] > hv) my_edges |= 1u;
                 }
             v = o[TH * P + x + 1];
-            if (!(v == sm.eS[x]))
+            if (fresh || !(v == sm.eS[x]))
                 for (int d = -c8; d <= c8; ++d) {
                     int h = x + d;
                     if (h < 0 || h >= TW) continue;
@@ -477,7 +624,7 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
         }
         for (int y = threadIdx.x; y < TH; y += NW * 32) {
             T v = o[(y + 1) * P + 1];
-            if (!(v == sm.eW[y]))
+            if (fresh || !(v == sm.eW[y]))
                 for (int d = -c8; d <= c8; ++d) {
                     int h = y + d;
                     if (h < 0 || h >= TH) continue;
@@ -485,7 +632,7 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
                     if (v > hv && sm.mW[h] > hv) my_edges |= 4u;
                 }
             v = o[(y + 1) * P + TW];
-            if (!(v == sm.eE[y]))
+            if (fresh || !(v == sm.eE[y]))
                 for (int d = -c8; d <= c8; ++d) {
                     int h = y + d;
                     if (h < 0 || h >= TH) continue;
@@ -496,13 +643,13 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
         if (c8 && threadIdx.x == 0) {
             T v, hv;
             v = o[P + 1], hv = o[0];
-            if (!(v == sm.eN[0]) && v > hv && sm.mN[0] > hv) my_edges |= 32u;  // up-left
+            if ((fresh || !(v == sm.eN[0])) && v > hv && sm.mN[0] > hv) my_edges |= 32u;  // up-left
             v = o[P + TW], hv = o[TW + 1];
-            if (!(v == sm.eN[TW - 1]) && v > hv && sm.mN[TW + 1] > hv) my_edges |= 64u;  // up-right
+            if ((fresh || !(v == sm.eN[TW - 1])) && v > hv && sm.mN[TW + 1] > hv) my_edges |= 64u;  // up-right
             v = o[TH * P + 1], hv = o[(TH + 1) * P];
-            if (!(v == sm.eS[0]) && v > hv && sm.mS[0] > hv) my_edges |= 128u;  // down-left
+            if ((fresh || !(v == sm.eS[0])) && v > hv && sm.mS[0] > hv) my_edges |= 128u;  // down-left
             v = o[TH * P + TW], hv = o[(TH + 1) * P + TW + 1];
-            if (!(v == sm.eS[TW - 1]) && v > hv && sm.mS[TW + 1] > hv) my_edges |= 256u;  // down-right
+            if ((fresh || !(v == sm.eS[TW - 1])) && v > hv && sm.mS[TW + 1] > hv) my_edges |= 256u;  // down-right
         }
     }
     if (my_edges) atomicOr(&sm.edges, (int)my_edges);
@@ -590,8 +737,30 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
         init_min_f32<<<blocks, 256, 0, s>>>((const float *)marker, (const float *)mask, (float *)out, n);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
-    init_queue<<<(qcap + 255) / 256, 256, 0, s>>>(state, queue, dirty, qcap, ntiles, c.ws.ctrl);
-    NSG_COUNT_LAUNCH();
+    // Whole-image row + column sweep pairs before the tile queue.  Off by
+    // default: a thread per line walks the line serially, and on the tiles of
+    // this pipeline a pair costs more than the tile passes it saves.
+    int nsweep = 0;
+    if (const char *e = getenv("NSG_RECON_SWEEPS")) nsweep = atoi(e);  // tuning knob (0: tile queue only)
+    if (nsweep <= 0) {
+        init_queue<<<(qcap + 255) / 256, 256, 0, s>>>(state, queue, dirty, qcap, ntiles, c.ws.ctrl);
+        NSG_COUNT_LAUNCH();
+    } else {
+        int *changed = c.ws.ctrl + C_RSTATS + 2;
+        zero_ints<<<(ntiles + 255) / 256, 256, 0, s>>>(dirty, ntiles);
+        NSG_COUNT_LAUNCH();
+        NSG_CUDA_TRY(c, cudaMemsetAsync(changed, 0, sizeof(int), s));
+        const int c8 = conn == 8;
+        for (int k = 0; k < nsweep; ++k) {
+            sweep_rows<T><<<(rows + 127) / 128, 128, 0, s>>>(mask, out, rows, cols, c8, changed);
+            NSG_COUNT_LAUNCH();
+            sweep_cols<T><<<(cols + 127) / 128, 128, 0, s>>>(mask, out, rows, cols, c8, changed,
+                                                             k + 1 == nsweep ? dirty : nullptr, TW, TH, tiles_x);
+            NSG_COUNT_LAUNCH();
+        }
+        queue_marked<<<1, 1024, 0, s>>>(state, queue, dirty, qcap, ntiles, c.ws.ctrl);
+        NSG_COUNT_LAUNCH();
+    }
     NSG_LAUNCH_CHECK(c);
     Queue q;
     q.state = state;

@@ -47,3 +47,21 @@ def test_product_does_not_link_the_oracle(nsg):
     assert "orc_" not in out and "ref_cc_" not in out
     deps = subprocess.run(["ldd", _lib.LIB_PATH], capture_output=True, text=True).stdout
     assert "oracle" not in deps and "torch" not in deps
+
+
+def test_pool_and_server_host_checks(nsg):
+    """Sizes and admission are decided on the host, before any device call."""
+    import ctypes as C
+    from nscale_gb300 import _lib
+    per = nsg.nsg_pool_context_bytes(4096, 4096)
+    assert per > 16 * 4096 * 4096  # several planes of the padded image
+    assert nsg.nsg_pool_context_bytes(2048, 2048) < per
+    assert nsg.nsg_pool_context_bytes(0, 10) == 0
+    h = C.c_void_p()
+    # a budget that does not hold one tile's workspace is refused
+    assert nsg.nsg_server_create(C.byref(h), 4096, 4096, per - 1, 8, 0) == _lib.ERR_OOM
+    assert nsg.nsg_server_create(C.byref(h), 4096, 4096, per, 0, 0) == _lib.ERR_ARG
+    assert nsg.nsg_pool_create(C.byref(h), 512, 512, 0, 0) == _lib.ERR_ARG
+    assert nsg.nsg_pool_destroy(None) == _lib.ERR_ARG
+    assert nsg.nsg_server_destroy(None) == _lib.ERR_ARG
+    assert nsg.nsg_segment_nuclei_batch(None, None, 0, None, 0) == _lib.ERR_ARG

@@ -1,0 +1,110 @@
+"""The batched form (nsg_segment_nuclei_batch) and the in-process server
+(nsg_server_*) must give every tile exactly what a plain per-tile call gives,
+whatever else is in flight (alone-vs-mix equality), and the per-tile call is
+itself pinned to the oracle by test_gpu_pipeline."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(512, 512), (700, 1100), (1024, 768), (333, 1500), (900, 900)]
+
+
+def _tiles():
+    from nscale_gb300 import synth
+    out = [synth.he_tile(r, c, seed=0x5EED7000 + i) for i, (r, c) in enumerate(SHAPES)]
+    out.append(synth.white_tile(400, 600, seed=0x5EED7100))  # BACKGROUND early exit
+    return out
+
+
+def _single(img):
+    import torch
+    from nscale_gb300.histological_entities import HistologicalEntities as HE
+    st, lab, n, bb = HE.segmentNuclei(torch.from_numpy(img).cuda())
+    torch.cuda.synchronize()
+    return st, lab.cpu().numpy(), n, bb
+
+
+def test_batch_matches_per_tile_device_and_host(cuda):
+    import torch
+    from nscale_gb300.serving import TilePool
+    tiles = _tiles()
+    want = [_single(t) for t in tiles]
+    pool = TilePool(1024, 1500, workers=3)
+    try:
+        dev = pool.segment([torch.from_numpy(t).cuda() for t in tiles])
+        host = pool.segment(tiles)
+        for got in (dev, host):
+            for (ws, wl, wn, wb), (gs, gl, gn, gb) in zip(want, got):
+                gl = gl.cpu().numpy() if hasattr(gl, "cpu") else gl
+                assert gs == ws and gn == wn
+                assert np.array_equal(gl, wl)
+                assert np.array_equal(gb, wb)
+    finally:
+        pool.close()
+    assert {w[0] for w in want} >= {0, 1}  # the mix holds a SUCCESS and a BACKGROUND tile
+
+
+def test_server_alone_vs_mix(cuda):
+    from nscale_gb300 import _lib
+    from nscale_gb300.serving import TileServer
+    tiles = _tiles()
+    per = _lib.load().nsg_pool_context_bytes(1024, 1500)
+    # alone: a one-worker server, one tile at a time
+    alone = []
+    srv = TileServer(1024, 1500, per, queue_cap=4)
+    assert srv.workers == 1
+    try:
+        for t in tiles:
+            lab = np.empty(t.shape[:2], np.int32)
+            k = srv.submit(t, lab, want_bbox=True)
+            (r,) = srv.poll(1, 60000)
+            assert r["ticket"] == k
+            alone.append((r["status"], lab, r["compcount"], r["bbox"]))
+    finally:
+        srv.close()
+    # mix: three workers, every tile submitted twice, interleaved
+    srv = TileServer(1024, 1500, 3 * per + per // 2, queue_cap=64)
+    assert srv.workers == 3
+    try:
+        order = list(range(len(tiles))) * 2
+        tick = {}
+        for i in order:
+            lab = np.empty(tiles[i].shape[:2], np.int32)
+            tick[srv.submit(tiles[i], lab, want_bbox=True)] = (i, lab)
+        got = []
+        while len(got) < len(order):
+            got += srv.poll(16, 60000)
+        for r in got:
+            i, lab = tick[r["ticket"]]
+            assert r["labels"] is lab
+            st, wl, wn, wb = alone[i]
+            assert r["status"] == st and r["compcount"] == wn
+            assert np.array_equal(lab, wl) and np.array_equal(r["bbox"], wb)
+            assert r["latency_ms"] > 0
+    finally:
+        srv.close()
+
+
+def test_server_queue_bound(cuda):
+    from nscale_gb300 import _lib, synth
+    from nscale_gb300.serving import TileServer
+    per = _lib.load().nsg_pool_context_bytes(2048, 2048)
+    srv = TileServer(2048, 2048, per, queue_cap=1)
+    big = synth.he_tile(2048, 2048, seed=0x5EED7200)
+    try:
+        accepted, refused = 0, 0
+        for _ in range(40):
+            try:
+                srv.submit(big, None)
+                accepted += 1
+            except _lib.NsgError as e:
+                assert e.code == _lib.ERR_QUEUE_FULL
+                refused += 1
+        assert refused > 0 and accepted >= 1
+        got = []
+        while len(got) < accepted:
+            got += srv.poll(8, 60000)
+        assert all(r["status"] == 0 for r in got)
+    finally:
+        srv.close()
