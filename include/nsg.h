@@ -184,6 +184,20 @@ int nsg_watershed_diagnostics(nsg_context *ctx, int *out16, nsg_stream_t stream)
 int nsg_bounding_box(nsg_context *ctx, const int32_t *labels, int rows, int cols, int32_t *bbox_out, int capacity,
                      int *compcount, nsg_stream_t stream);
 
+/* ---- PixelOperations colour deconvolution (features input) ---------------- */
+/* PixelOperations::ComputeInverseStainMatrix (PixelOperations.cpp:94-156):
+ * the rows of inv(normalised M) selected by b, as float, row-major 2 x 3
+ * (columns R, G, B).  M is 3 x 3 row-major (rows R, G, B; columns stains);
+ * NULL M / b = the feature pipeline's stains (nu-features.cpp:691-692).
+ * Host only. */
+int nsg_stain_matrix(const double *M9, const uint8_t *b3, float *Q6);
+/* PixelOperations::ColorDeconv(image, Q, lut, H, E, BGR2RGB = true)
+ * (PixelOperations.cpp:170-274) with ComputeLookupTable's optical-density
+ * table (:158-168): uint8 hematoxylin H and eosin E (either nullable).  Q6 is
+ * host memory (nsg_stain_matrix's output). */
+int nsg_color_deconv(nsg_context *ctx, const uint8_t *bgr, int rows, int cols, size_t row_stride_bytes,
+                     const float *Q6, uint8_t *H, uint8_t *E, nsg_stream_t stream);
+
 /* ---- HistologicalEntities::segmentNuclei ----------------------------------- */
 /* segmentNuclei(img, output, compcount, bbox, params...) (HistologicalEntities.cpp:473-598)
  * and the mask-only overload (HistologicalEntities.cpp:600-664).

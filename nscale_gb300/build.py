@@ -17,6 +17,7 @@ OUT = os.path.join(HERE, "libnsg.so")
 OBJ = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
+         "-Xcompiler", "-ffp-contract=off",  # host double math rounds like the oracle's (no fused multiply-add)
          "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 

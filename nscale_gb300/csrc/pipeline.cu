@@ -488,6 +488,26 @@ int nsg_watershed_diagnostics(nsg_context *h, int *out16, nsg_stream_t s) {
     return watershed_diag(h->c, out16, S(s));
 }
 
+int nsg_stain_matrix(const double *M9, const uint8_t *b3, float *Q6) {
+    if (!Q6) return NSG_ERR_ARG;
+    static const double kM[9] = {0.650, 0.072, 0, 0.704, 0.990, 0, 0.286, 0.105, 0};  // nu-features.cpp:691-692
+    static const uint8_t kB[3] = {1, 1, 0};
+    double q[6];
+    if (stain_matrix(M9 ? M9 : kM, b3 ? b3 : kB, q) != 2) return NSG_ERR_ARG;
+    for (int i = 0; i < 6; ++i) Q6[i] = (float)q[i];
+    return NSG_SUCCESS;
+}
+
+int nsg_color_deconv(nsg_context *h, const uint8_t *bgr, int rows, int cols, size_t row_stride_bytes,
+                     const float *Q6, uint8_t *H, uint8_t *E, nsg_stream_t s) {
+    return run_op(h, s, [&](Ctx &c) {
+        NSG_TRY(check_dims(c, rows, cols));
+        const int64_t stride = row_stride_bytes ? (int64_t)row_stride_bytes : (int64_t)cols * 3;
+        if (!bgr || !Q6 || stride < (int64_t)cols * 3) return NSG_ERR_ARG;
+        return color_deconv_dev(c, bgr, stride, rows, cols, Q6, H, E, S(s));
+    });
+}
+
 int nsg_bounding_box(nsg_context *h, const int32_t *labels, int rows, int cols, int32_t *bbox_out, int capacity,
                      int *compcount, nsg_stream_t s) {
     int r = run_op(h, s, [&](Ctx &c) {

@@ -84,6 +84,37 @@ class HistologicalEntities:
 
 class PixelOperations:
     @staticmethod
+    def ComputeInverseStainMatrix(M=None, b=None) -> np.ndarray:
+        """PixelOperations.cpp:94-156: float32 (2, 3), columns R, G, B.  None =
+        the feature pipeline's stains (nu-features.cpp:691-692)."""
+        L = _lib.load()
+        q = (C.c_float * 6)()
+        Mp = np.ascontiguousarray(M, np.float64).ravel() if M is not None else None
+        bp = np.ascontiguousarray(b, np.uint8).ravel() if b is not None else None
+        rc = L.nsg_stain_matrix(Mp.ctypes.data if Mp is not None else None,
+                                bp.ctypes.data if bp is not None else None, q)
+        if rc < 0:
+            raise _lib.NsgError(rc, "stain matrix")
+        return np.array(q[:], np.float32).reshape(2, 3)
+
+    @staticmethod
+    def ColorDeconv(image, Q=None):
+        """PixelOperations::ColorDeconv(image, Q, lut, H, E, BGR2RGB = true)
+        (PixelOperations.cpp:170-274): uint8 H and E CUDA tensors."""
+        if isinstance(image, np.ndarray):
+            image = torch.from_numpy(np.ascontiguousarray(image)).cuda()
+        image = _bgr(image)
+        rows, cols = image.shape[:2]
+        q = np.ascontiguousarray(PixelOperations.ComputeInverseStainMatrix() if Q is None else Q, np.float32)
+        ctx = get_context(rows, cols)
+        H = torch.empty((rows, cols), dtype=torch.uint8, device=image.device)
+        E = torch.empty_like(H)
+        qp = q.ravel().ctypes.data_as(C.POINTER(C.c_float))
+        ctx.check(ctx.L.nsg_color_deconv(ctx.h, ptr(image), rows, cols, cols * 3, qp, ptr(H), ptr(E),
+                                         stream_handle()))
+        return H, E
+
+    @staticmethod
     def invert(img: torch.Tensor) -> torch.Tensor:
         """PixelOperations.cpp:22-43 (uint8: 255 - x)."""
         if img.dtype != torch.uint8:

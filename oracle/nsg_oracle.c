@@ -1048,3 +1048,118 @@ done:
     if (!labels_out) free(labels);
     return status;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Colour deconvolution, PixelOperations.cpp:94-274.                         */
+/* ------------------------------------------------------------------------- */
+
+/* PixelOperations::ComputeInverseStainMatrix (PixelOperations.cpp:94-156):
+ * normalise each stain column of M (3x3, row-major) to unit length; if the
+ * last column is zero, fill it row by row with sqrt(1 - |row|^2) (0 when the
+ * row norm exceeds 1) and normalise it; invert; keep the rows i with
+ * b[i] == 1.  Q6 receives up to two rows of 3 (the reference drops the first
+ * row of its gathered matrix, which is a placeholder).  Returns the number of
+ * rows kept.  The inverse is Gaussian elimination with partial pivoting, the
+ * method OpenCV's Mat::inv (DECOMP_LU) uses. */
+int orc_stain_matrix(const double *M9, const uint8_t *b3, double *Q6) {
+    double N[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) N[r][c] = M9[r * 3 + c];
+    for (int c = 0; c < 3; ++c) {
+        double nrm = sqrt(N[0][c] * N[0][c] + N[1][c] * N[1][c] + N[2][c] * N[2][c]);
+        if (nrm > 0)
+            for (int r = 0; r < 3; ++r) N[r][c] /= nrm;
+    }
+    double last = sqrt(N[0][2] * N[0][2] + N[1][2] * N[1][2] + N[2][2] * N[2][2]);
+    if (last == 0) {
+        for (int r = 0; r < 3; ++r) {
+            double nrm = sqrt(N[r][0] * N[r][0] + N[r][1] * N[r][1] + N[r][2] * N[r][2]);
+            N[r][2] = nrm > 1 ? 0 : sqrt(1 - nrm * nrm);
+        }
+        double n2 = sqrt(N[0][2] * N[0][2] + N[1][2] * N[1][2] + N[2][2] * N[2][2]);
+        if (n2 == 0) return 0;
+        for (int r = 0; r < 3; ++r) N[r][2] /= n2;
+    }
+    /* [N | I] -> [I | inv(N)] */
+    double A[3][6];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 6; ++c) A[r][c] = c < 3 ? N[r][c] : (c - 3 == r ? 1.0 : 0.0);
+    for (int k = 0; k < 3; ++k) {
+        int piv = k;
+        for (int r = k + 1; r < 3; ++r)
+            if (fabs(A[r][k]) > fabs(A[piv][k])) piv = r;
+        if (A[piv][k] == 0) return 0;
+        if (piv != k)
+            for (int c = 0; c < 6; ++c) {
+                double t = A[k][c];
+                A[k][c] = A[piv][c];
+                A[piv][c] = t;
+            }
+        double d = A[k][k];
+        for (int c = 0; c < 6; ++c) A[k][c] /= d;
+        for (int r = 0; r < 3; ++r) {
+            if (r == k) continue;
+            double f = A[r][k];
+            for (int c = 0; c < 6; ++c) A[r][c] -= f * A[k][c];
+        }
+    }
+    int kept = 0;
+    for (int i = 0; i < 3 && kept < 2; ++i)
+        if (b3[i] == 1) {
+            for (int c = 0; c < 3; ++c) Q6[kept * 3 + c] = A[i][3 + c];
+            ++kept;
+        }
+    return kept;
+}
+
+/* PixelOperations::ComputeLookupTable (PixelOperations.cpp:158-168):
+ * k = (float)(-255/ln 255); lut[i] = (float)(k * ln(i + 1) + 255) in double. */
+void orc_color_lut(float *lut) {
+    const float k = (float)(-255.0 / log(255.0));
+    for (int i = 0; i < 256; ++i) lut[i] = (float)((double)k * log((double)(float)i + 1.0) + 255.0);
+}
+
+static uint8_t sat_round_u8(float v) { /* saturate_cast<uchar>(float): round half to even, clamp */
+    long r = lrintf(v);
+    return (uint8_t)(r < 0 ? 0 : (r > 255 ? 255 : r));
+}
+
+/* PixelOperations::ColorDeconv(image, Q, lut, H, E, BGR2RGB = true)
+ * (PixelOperations.cpp:170-274): dn = lut[BGR]; cn = dn * flip(Q^T) (the
+ * float matrix product, whose 32-bit products OpenCV 2.4 sums in double:
+ * restated, unpinned), i.e. cn_j = dn_B * Q[j][B] + dn_G * Q[j][G] +
+ * dn_R * Q[j][R] in that order; out = saturate_u8(expf((cn - 255) *
+ * (float)(-ln 255 / 255))). */
+void orc_color_deconv(const uint8_t *bgr, int rows, int cols, const float *Q6, const float *lut, uint8_t *H,
+                      uint8_t *E) {
+    const float c = (float)(-log(255.0) / 255.0);
+    const int64_t n = (int64_t)rows * cols;
+    for (int64_t i = 0; i < n; ++i) {
+        const float db = lut[bgr[3 * i]], dg = lut[bgr[3 * i + 1]], dr = lut[bgr[3 * i + 2]];
+        for (int j = 0; j < 2; ++j) {
+            double acc = (double)db * (double)Q6[j * 3 + 2];
+            acc += (double)dg * (double)Q6[j * 3 + 1];
+            acc += (double)dr * (double)Q6[j * 3 + 0];
+            const float cn = (float)acc;
+            const float v = expf((cn - 255.0f) * c);
+            (j == 0 ? H : E)[i] = sat_round_u8(v);
+        }
+    }
+}
+
+/* the same in double throughout (the reference's GPU path computes in FP64):
+ * the FP oracle for flip counts */
+void orc_color_deconv_f64(const uint8_t *bgr, int rows, int cols, const double *Q6, uint8_t *H, uint8_t *E) {
+    const double k = -255.0 / log(255.0), c = -log(255.0) / 255.0;
+    const int64_t n = (int64_t)rows * cols;
+    for (int64_t i = 0; i < n; ++i) {
+        const double db = k * log(bgr[3 * i] + 1.0) + 255.0, dg = k * log(bgr[3 * i + 1] + 1.0) + 255.0,
+                     dr = k * log(bgr[3 * i + 2] + 1.0) + 255.0;
+        for (int j = 0; j < 2; ++j) {
+            const double cn = db * Q6[j * 3 + 2] + dg * Q6[j * 3 + 1] + dr * Q6[j * 3 + 0];
+            double v = exp((cn - 255.0) * c);
+            v = v < 0 ? 0 : (v > 255 ? 255 : v);
+            (j == 0 ? H : E)[i] = (uint8_t)lrint(v);
+        }
+    }
+}

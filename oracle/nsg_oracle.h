@@ -115,6 +115,14 @@ void orc_watershed2(const uint8_t *bgr, const float *img, int rows, int cols, in
 int orc_bounding_box(const int32_t *labels, int w, int h, int32_t *bbox_out);
 int orc_bounding_box_refbug(const int32_t *labels, int w, int h, int bgval, int32_t *bbox_out);
 
+/* Colour deconvolution (PixelOperations.cpp:94-274), not part of segmentNuclei;
+ * the per-nucleus features of the serving configuration read its H channel. */
+int orc_stain_matrix(const double *M9, const uint8_t *b3, double *Q6);  /* rows of inv(normalised M) picked by b */
+void orc_color_lut(float *lut256);
+void orc_color_deconv(const uint8_t *bgr, int rows, int cols, const float *Q6, const float *lut256, uint8_t *H,
+                      uint8_t *E);
+void orc_color_deconv_f64(const uint8_t *bgr, int rows, int cols, const double *Q6, uint8_t *H, uint8_t *E);
+
 int orc_segment_nuclei(const uint8_t *bgr, int rows, int cols, const orc_params *p,
                        int32_t *labels_out, uint8_t *mask_out, int *compcount, int32_t *bbox_out,
                        orc_dump *dump);

@@ -76,6 +76,12 @@ def lib():
         L.orc_get_background.argtypes = [_u8p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
         L.orc_get_rbc.argtypes = [_u8p, C.c_int, C.c_int, C.c_double, C.c_double, _u8p]
         L.orc_get_rbc_f64.argtypes = [_u8p, C.c_int, C.c_int, C.c_double, C.c_double, _u8p]
+        _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+        L.orc_stain_matrix.argtypes = [_f64p, _u8p, _f64p]
+        L.orc_stain_matrix.restype = C.c_int
+        L.orc_color_lut.argtypes = [_f32p]
+        L.orc_color_deconv.argtypes = [_u8p, C.c_int, C.c_int, _f32p, _f32p, _u8p, _u8p]
+        L.orc_color_deconv_f64.argtypes = [_u8p, C.c_int, C.c_int, _f64p, _u8p, _u8p]
         L.orc_erode_u8.argtypes = [_u8p, C.c_int, C.c_int, _u8p, C.c_int, _u8p]
         L.orc_dilate_u8.argtypes = [_u8p, C.c_int, C.c_int, _u8p, C.c_int, _u8p]
         L.orc_morph_open_u8.argtypes = [_u8p, C.c_int, C.c_int, _u8p, C.c_int, _u8p]
@@ -152,6 +158,39 @@ def get_rbc(bgr, T1=5.0, T2=4.0, f64=False):
     out = np.empty(bgr.shape[:2], np.uint8)
     (lib().orc_get_rbc_f64 if f64 else lib().orc_get_rbc)(bgr, bgr.shape[0], bgr.shape[1], T1, T2, out)
     return out
+
+
+# the feature pipeline's stains and selector (nu-features.cpp:691-692)
+STAINS_M = np.array([[0.650, 0.072, 0], [0.704, 0.990, 0], [0.286, 0.105, 0]], np.float64)
+STAINS_B = np.array([1, 1, 0], np.uint8)
+
+
+def stain_matrix(M=STAINS_M, b=STAINS_B):
+    """PixelOperations::ComputeInverseStainMatrix (PixelOperations.cpp:94-156), in double (2 x 3)."""
+    q = np.empty(6, np.float64)
+    kept = lib().orc_stain_matrix(_c(M, np.float64).ravel(), _c(b, np.uint8), q)
+    assert kept == 2
+    return q.reshape(2, 3)
+
+
+def color_lut():
+    lut = np.empty(256, np.float32)
+    lib().orc_color_lut(lut)
+    return lut
+
+
+def color_deconv(bgr, Q=None, f64=False):
+    """PixelOperations::ColorDeconv(BGR2RGB = true) -> (H, E) uint8; f64 = all in double."""
+    bgr = _c(bgr, np.uint8)
+    Qd = stain_matrix() if Q is None else np.asarray(Q, np.float64)
+    H = np.empty(bgr.shape[:2], np.uint8)
+    E = np.empty_like(H)
+    if f64:
+        lib().orc_color_deconv_f64(bgr, bgr.shape[0], bgr.shape[1], _c(Qd, np.float64).ravel(), H, E)
+    else:
+        lib().orc_color_deconv(bgr, bgr.shape[0], bgr.shape[1], _c(Qd.astype(np.float32), np.float32).ravel(),
+                               color_lut(), H, E)
+    return H, E
 
 
 def erode(img, se):

@@ -285,3 +285,23 @@ def test_watershed_adversarial_small(cuda, orc):
         paths[_ws_diag()[0]] = paths.get(_ws_diag()[0], 0) + 1
         np.testing.assert_array_equal(got, orc.watershed2(bgr, d2, 8 if it % 2 else 4), err_msg=f"case {it}")
     assert paths.get(0, 0) > 0
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (97, 131), (512, 700)])
+def test_color_deconv(cuda, orc, shape):
+    """ColorDeconv (PixelOperations.cpp:170-274) against the FP32 oracle.  The
+    optical-density table, the stain matrix and the double-summed products
+    are bit-exact; expf may differ from the host's in the last bit, so a grey
+    level may flip at a rounding boundary: tolerance 1 level on at most 0.01 %
+    of pixels."""
+    from nscale_gb300 import synth
+    from nscale_gb300.histological_entities import PixelOperations as PO
+    img = synth.he_tile(*shape, seed=0x5EED0A00 + shape[0])
+    q = PO.ComputeInverseStainMatrix()
+    assert np.array_equal(q, orc.stain_matrix().astype(np.float32))
+    H, E = PO.ColorDeconv(T(img))
+    oH, oE = orc.color_deconv(img)
+    for g, o in ((N(H), oH), (N(E), oE)):
+        d = np.abs(g.astype(int) - o.astype(int))
+        assert d.max() <= 1
+        assert (d > 0).sum() <= max(0, int(1e-4 * d.size))

@@ -177,3 +177,33 @@ def test_segment_background_status(orc):
     from nscale_gb300 import synth
     st, lab, _, bbox, _ = orc.segment_nuclei(synth.white_tile(64, 80, seed=1))
     assert st == 1 and (lab == -1).all() and bbox.shape == (5, 0)
+
+
+def test_color_lut_and_stain_matrix(orc):
+    """ComputeLookupTable / ComputeInverseStainMatrix (PixelOperations.cpp:94-168)
+    against a numpy restatement in double."""
+    k = np.float32(-255.0 / np.log(255.0))
+    want = (np.float64(k) * np.log(np.arange(256, dtype=np.float32).astype(np.float64) + 1.0) + 255.0)
+    assert np.array_equal(orc.color_lut(), want.astype(np.float32))
+    M = orc.STAINS_M.copy()
+    N = M / np.maximum(np.linalg.norm(M, axis=0), 1e-300)
+    N[:, 2] = 0
+    rn = np.linalg.norm(N, axis=1)
+    N[:, 2] = np.where(rn > 1, 0, np.sqrt(np.maximum(0, 1 - rn * rn)))
+    N[:, 2] /= np.linalg.norm(N[:, 2])
+    Q = np.linalg.inv(N)[:2]
+    assert np.allclose(orc.stain_matrix(), Q, rtol=1e-12, atol=1e-14)
+
+
+def test_color_deconv_fp32_vs_fp64(orc):
+    """FP oracle: the FP32 path (the reference CPU's) against the FP64 one:
+    at most one grey level apart, on a small fraction of pixels."""
+    from nscale_gb300 import synth
+    img = synth.he_tile(256, 320, seed=0x5EED0A22)
+    H32, E32 = orc.color_deconv(img)
+    H64, E64 = orc.color_deconv(img, f64=True)
+    for a, b in ((H32, H64), (E32, E64)):
+        d = np.abs(a.astype(int) - b.astype(int))
+        assert d.max() <= 1
+        assert (d > 0).mean() < 0.01
+    assert H32.std() > 5  # the channel carries the nuclei
