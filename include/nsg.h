@@ -198,6 +198,22 @@ int nsg_stain_matrix(const double *M9, const uint8_t *b3, float *Q6);
 int nsg_color_deconv(nsg_context *ctx, const uint8_t *bgr, int rows, int cols, size_t row_stride_bytes,
                      const float *Q6, uint8_t *H, uint8_t *E, nsg_stream_t stream);
 
+/* ---- per-nucleus features (the serving output) ---------------------------- */
+/* Operators::gradient (Operators.cpp:568-640): |grad| of a uint8 image,
+ * central differences with one-sided ones at the edges, rounded to uint8. */
+int nsg_gradient_u8(nsg_context *ctx, const uint8_t *in, uint8_t *out, int rows, int cols, nsg_stream_t stream);
+/* For every component of a -1-background label image (bounding-box order =
+ * increasing label), NSG_N_FEATURES floats into DEVICE `features`:
+ * area (ObjFeatures::area, ObjFeatures.cpp:15-43), perimeter
+ * (ObjFeatures::perimeter, :143-270), mean and std of `gray` and mean of its
+ * gradient (intensityFeatures / gradientFeatures, :342-418, histogram
+ * statistics of Operators.cpp:281-313).  `gray` is normally the H channel of
+ * nsg_color_deconv.  *count (host) receives the number of components;
+ * NSG_ERR_ARG when it exceeds `capacity`. */
+#define NSG_N_FEATURES 5
+int nsg_nucleus_features(nsg_context *ctx, const int32_t *labels, const uint8_t *gray, int rows, int cols,
+                         float *features, int capacity, int *count, nsg_stream_t stream);
+
 /* ---- HistologicalEntities::segmentNuclei ----------------------------------- */
 /* segmentNuclei(img, output, compcount, bbox, params...) (HistologicalEntities.cpp:473-598)
  * and the mask-only overload (HistologicalEntities.cpp:600-664).

@@ -104,6 +104,9 @@ namespace nsg {
 int stain_matrix(const double *M9, const uint8_t *b3, double *Q6);
 int color_deconv_dev(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int cols, const float *Q6, uint8_t *H,
                      uint8_t *E, cudaStream_t s);
+int gradient_dev(Ctx &c, const uint8_t *in, uint8_t *out, int rows, int cols, cudaStream_t s);
+int nucleus_features_dev(Ctx &c, const int32_t *labels, const uint8_t *gray, int rows, int cols, float *out,
+                         int capacity, int *count, cudaStream_t s);
 // device bytes of a context for images up to max_rows x max_cols
 size_t context_bytes_for(int max_rows, int max_cols);
 int segment_nuclei_dev(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int cols, const nsg_seg_params &p,

@@ -508,6 +508,26 @@ int nsg_color_deconv(nsg_context *h, const uint8_t *bgr, int rows, int cols, siz
     });
 }
 
+int nsg_gradient_u8(nsg_context *h, const uint8_t *in, uint8_t *out, int rows, int cols, nsg_stream_t s) {
+    return run_op(h, s, [&](Ctx &c) {
+        NSG_TRY(check_dims(c, rows, cols));
+        if (!in || !out) return NSG_ERR_ARG;
+        return gradient_dev(c, in, out, rows, cols, S(s));
+    });
+}
+
+int nsg_nucleus_features(nsg_context *h, const int32_t *labels, const uint8_t *gray, int rows, int cols,
+                         float *features, int capacity, int *count, nsg_stream_t s) {
+    int cnt = 0;
+    int r = run_op(h, s, [&](Ctx &c) {
+        NSG_TRY(check_dims(c, rows, cols));
+        if (!labels || !gray || (!features && capacity > 0) || capacity < 0) return NSG_ERR_ARG;
+        return nucleus_features_dev(c, labels, gray, rows, cols, features, capacity, &cnt, S(s));
+    });
+    if (count) *count = cnt;
+    return r;
+}
+
 int nsg_bounding_box(nsg_context *h, const int32_t *labels, int rows, int cols, int32_t *bbox_out, int capacity,
                      int *compcount, nsg_stream_t s) {
     int r = run_op(h, s, [&](Ctx &c) {

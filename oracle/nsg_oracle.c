@@ -1163,3 +1163,135 @@ void orc_color_deconv_f64(const uint8_t *bgr, int rows, int cols, const double *
         }
     }
 }
+
+/* ------------------------------------------------------------------------- */
+/* Per-nucleus features (src/features/ObjFeatures.cpp, Operators.cpp).       */
+/* ------------------------------------------------------------------------- */
+
+/* rndint (Operators.cpp:554-564): floor, plus one when the fraction >= 0.5 */
+static int feat_rndint(float n) {
+    int ret = (int)floorf(n);
+    float t = n - floorf(n);
+    if (t >= 0.5f) ret = (int)floorf(n) + 1;
+    return ret;
+}
+
+/* Operators::gradient (Operators.cpp:568-640): correlation with
+ * [-0.5, 0, 0.5] along x and along y (cvFilter2D, replicated border), the
+ * first and last column (row) doubled, magnitude sqrt(dx^2 + dy^2) in float,
+ * then rndint and clamp to uint8. */
+void orc_gradient_u8(const uint8_t *in, int rows, int cols, uint8_t *out) {
+    for (int y = 0; y < rows; ++y)
+        for (int x = 0; x < cols; ++x) {
+            const int xl = x > 0 ? x - 1 : 0, xr = x + 1 < cols ? x + 1 : cols - 1;
+            const int yu = y > 0 ? y - 1 : 0, yd = y + 1 < rows ? y + 1 : rows - 1;
+            float dx = -0.5f * (float)in[(int64_t)y * cols + xl] + 0.5f * (float)in[(int64_t)y * cols + xr];
+            float dy = -0.5f * (float)in[(int64_t)yu * cols + x] + 0.5f * (float)in[(int64_t)yd * cols + x];
+            if (x == 0 || x == cols - 1) dx *= 2;
+            if (y == 0 || y == rows - 1) dy *= 2;
+            float acc = 0.0f;
+            acc += dx * dx;
+            acc += dy * dy;
+            const float m = sqrtf(acc);
+            out[(int64_t)y * cols + x] = m < 0.0f ? 0 : (m > 255.0f ? 255 : (uint8_t)feat_rndint(m));
+        }
+}
+
+/* Operators::calcMeanFromHistogram / calcStdFromHistogram (Operators.cpp:281-313) */
+static double feat_mean(const int *h) {
+    double m = 0.0;
+    int n = 0;
+    for (int i = 0; i < 256; ++i) {
+        m += h[i] * i;
+        n += h[i];
+    }
+    return n == 0 ? 0.0 : m / n;
+}
+static double feat_std(const int *h) {
+    double sum = 0.0, n = 0;
+    for (int i = 0; i < 256; ++i) {
+        sum += i * h[i];
+        n += h[i];
+    }
+    const double mean = sum / n;
+    double sq = 0.0;
+    for (int i = 0; i < 256; ++i) {
+        const double d = i - mean;
+        sq += d * d * h[i];
+    }
+    return sqrt(sq / n);
+}
+
+/* For every component of a -1-background label image, in bounding-box order
+ * (increasing label): ObjFeatures::area (ObjFeatures.cpp:15-43),
+ * ObjFeatures::perimeter (:143-270, marching squares over the box and its
+ * one-pixel ring, summed in the reference's order), and the histogram mean /
+ * std of `gray` (intensityFeatures, :342-375) and the histogram mean of its
+ * gradient (gradientFeatures, :377-418).  feat5 receives 5 floats per
+ * component; returns the component count. */
+int orc_nucleus_features(const int32_t *labels, const uint8_t *gray, int rows, int cols, float *feat5) {
+    const int64_t n = (int64_t)rows * cols;
+    int32_t *bb = (int32_t *)malloc(sizeof(int32_t) * 5 * (size_t)(n > 0 ? n : 1));
+    const int cnt = orc_bounding_box(labels, cols, rows, bb);
+    uint8_t *grad = (uint8_t *)malloc((size_t)(n > 0 ? n : 1));
+    orc_gradient_u8(gray, rows, cols, grad);
+    static const double lut[16] = {0.0,          0.70710678118, 0.70710678118, 1.0,
+                                   0.70710678118, 1.41421356237, 1.0,           0.70710678118,
+                                   0.70710678118, 1.0,           1.41421356237, 0.70710678118,
+                                   1.0,           0.70710678118, 0.70710678118, 0.0};
+    int hg[256], hd[256];
+    for (int i = 0; i < cnt; ++i) {
+        /* the five arrays of the box buffer: label, minx, maxx, miny, maxy */
+        const int L = bb[i], x0 = bb[cnt + i], x1 = bb[2 * cnt + i], y0 = bb[3 * cnt + i], y1 = bb[4 * cnt + i];
+#define LB(yy, xx) (labels[(int64_t)(yy) * cols + (xx)] == L)
+        int area = 0;
+        memset(hg, 0, sizeof hg);
+        memset(hd, 0, sizeof hd);
+        for (int y = y0; y <= y1; ++y)
+            for (int x = x0; x <= x1; ++x)
+                if (LB(y, x)) {
+                    ++area;
+                    ++hg[gray[(int64_t)y * cols + x]];
+                    ++hd[grad[(int64_t)y * cols + x]];
+                }
+        double per = 0.0;
+        for (int y = y0; y < y1; ++y)
+            for (int x = x0; x < x1; ++x) {
+                int m = LB(y, x);
+                m = (m << 1) | LB(y, x + 1);
+                m = (m << 1) | LB(y + 1, x + 1);
+                m = (m << 1) | LB(y + 1, x);
+                per += lut[m];
+            }
+        for (int x = x0; x < x1; ++x) {
+            int m = LB(y1, x);
+            m = ((m << 1) | LB(y1, x + 1)) << 2;
+            per += lut[m];
+            m = LB(y0, x + 1);
+            m = (m << 1) | LB(y0, x);
+            per += lut[m];
+        }
+        for (int y = y0; y < y1; ++y) {
+            int m = LB(y, x0);
+            m = ((m << 1) | LB(y + 1, x0)) << 1;
+            per += lut[m];
+            m = LB(y, x1) << 2;
+            m = (m << 1) | LB(y + 1, x1);
+            per += lut[m];
+        }
+        per += lut[LB(y0, x0) << 1];
+        per += lut[LB(y0, x1)];
+        per += lut[LB(y1, x1) << 3];
+        per += lut[LB(y1, x0) << 2];
+#undef LB
+        float *f = feat5 + 5 * (int64_t)i;
+        f[0] = (float)area;
+        f[1] = (float)per;
+        f[2] = (float)feat_mean(hg);
+        f[3] = (float)feat_std(hg);
+        f[4] = (float)feat_mean(hd);
+    }
+    free(grad);
+    free(bb);
+    return cnt;
+}

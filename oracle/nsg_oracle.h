@@ -123,6 +123,12 @@ void orc_color_deconv(const uint8_t *bgr, int rows, int cols, const float *Q6, c
                       uint8_t *E);
 void orc_color_deconv_f64(const uint8_t *bgr, int rows, int cols, const double *Q6, uint8_t *H, uint8_t *E);
 
+/* Per-nucleus features of the serving output (src/features): gradient
+ * magnitude image (Operators.cpp:568-640) and, per label in bounding-box
+ * order, {area, perimeter, mean H, std H, mean gradient of H} as float. */
+void orc_gradient_u8(const uint8_t *in, int rows, int cols, uint8_t *out);
+int orc_nucleus_features(const int32_t *labels, const uint8_t *gray, int rows, int cols, float *feat5);
+
 int orc_segment_nuclei(const uint8_t *bgr, int rows, int cols, const orc_params *p,
                        int32_t *labels_out, uint8_t *mask_out, int *compcount, int32_t *bbox_out,
                        orc_dump *dump);

@@ -82,6 +82,9 @@ def lib():
         L.orc_color_lut.argtypes = [_f32p]
         L.orc_color_deconv.argtypes = [_u8p, C.c_int, C.c_int, _f32p, _f32p, _u8p, _u8p]
         L.orc_color_deconv_f64.argtypes = [_u8p, C.c_int, C.c_int, _f64p, _u8p, _u8p]
+        L.orc_gradient_u8.argtypes = [_u8p, C.c_int, C.c_int, _u8p]
+        L.orc_nucleus_features.argtypes = [_i32p, _u8p, C.c_int, C.c_int, _f32p]
+        L.orc_nucleus_features.restype = C.c_int
         L.orc_erode_u8.argtypes = [_u8p, C.c_int, C.c_int, _u8p, C.c_int, _u8p]
         L.orc_dilate_u8.argtypes = [_u8p, C.c_int, C.c_int, _u8p, C.c_int, _u8p]
         L.orc_morph_open_u8.argtypes = [_u8p, C.c_int, C.c_int, _u8p, C.c_int, _u8p]
@@ -191,6 +194,23 @@ def color_deconv(bgr, Q=None, f64=False):
         lib().orc_color_deconv(bgr, bgr.shape[0], bgr.shape[1], _c(Qd.astype(np.float32), np.float32).ravel(),
                                color_lut(), H, E)
     return H, E
+
+
+def gradient(img):
+    """Operators::gradient (Operators.cpp:568-640) -> uint8."""
+    img = _c(img, np.uint8)
+    out = np.empty_like(img)
+    lib().orc_gradient_u8(img, img.shape[0], img.shape[1], out)
+    return out
+
+
+def nucleus_features(labels, gray):
+    """(n, 5) float32: area, perimeter, mean gray, std gray, mean gradient, per
+    component in bounding-box order."""
+    labels, gray = _c(labels, np.int32), _c(gray, np.uint8)
+    out = np.empty((labels.size, 5), np.float32) if labels.size else np.empty((1, 5), np.float32)
+    n = lib().orc_nucleus_features(labels, gray, labels.shape[0], labels.shape[1], out.reshape(-1))
+    return out[:n].copy()
 
 
 def erode(img, se):

@@ -305,3 +305,24 @@ def test_color_deconv(cuda, orc, shape):
         d = np.abs(g.astype(int) - o.astype(int))
         assert d.max() <= 1
         assert (d > 0).sum() <= max(0, int(1e-4 * d.size))
+
+
+@pytest.mark.parametrize("shape", [(64, 80), (300, 411)])
+def test_gradient_and_nucleus_features(cuda, orc, shape):
+    """Operators::gradient bit-exact; per-nucleus area exact, the histogram
+    statistics exact as float, perimeter (counted cell classes against the
+    reference's ordered sum) within 1e-6 relative."""
+    from nscale_gb300 import synth
+    from nscale_gb300.features import ObjFeatures, Operators
+    from nscale_gb300.histological_entities import PixelOperations as PO
+    img = synth.he_tile(*shape, seed=0x5EEDF000 + shape[0])
+    H, _ = PO.ColorDeconv(T(img))
+    Hn = N(H)
+    assert np.array_equal(N(Operators.gradient(H)), orc.gradient(Hn))
+    lab = orc.bwlabel2(synth.disc_mask(*shape, seed=shape[1]), 8)
+    got = N(ObjFeatures.nucleusFeatures(T(lab), H))
+    want = orc.nucleus_features(lab, Hn)
+    assert got.shape == want.shape and len(want) > 0
+    assert np.array_equal(got[:, 0], want[:, 0])
+    assert np.allclose(got[:, 1], want[:, 1], rtol=1e-6, atol=0)
+    assert np.array_equal(got[:, 2:], want[:, 2:])

@@ -207,3 +207,58 @@ def test_color_deconv_fp32_vs_fp64(orc):
         assert d.max() <= 1
         assert (d > 0).mean() < 0.01
     assert H32.std() > 5  # the channel carries the nuclei
+
+
+def test_perimeter_known_answers(orc):
+    """ObjFeatures::perimeter (ObjFeatures.cpp:143-270) restated: a lone pixel
+    is four one-corner cells (4 / sqrt 2); a 2 x 2 block adds four edge cells."""
+    lab = np.full((6, 7), -1, np.int32)
+    lab[1, 1] = 8
+    lab[3:5, 3:5] = 24
+    f = orc.nucleus_features(lab, np.full(lab.shape, 100, np.uint8))
+    assert f.shape == (2, 5)
+    assert np.allclose(f[:, 0], [1, 4])
+    assert np.allclose(f[:, 1], [4 * 0.70710678118, 4 * 0.70710678118 + 4], rtol=1e-7)
+    assert np.allclose(f[:, 2], [100, 100]) and np.allclose(f[:, 3], [0, 0])
+
+
+def test_gradient_matches_numpy(orc):
+    """Operators::gradient: central differences, one-sided at the edges,
+    float magnitude rounded half up."""
+    rng = np.random.default_rng(5)
+    img = rng.integers(0, 256, (37, 53)).astype(np.uint8)
+    f = img.astype(np.float32)
+    dx = np.empty_like(f)
+    dy = np.empty_like(f)
+    dx[:, 1:-1] = (f[:, 2:] - f[:, :-2]) * np.float32(0.5)
+    dx[:, 0], dx[:, -1] = f[:, 1] - f[:, 0], f[:, -1] - f[:, -2]
+    dy[1:-1] = (f[2:] - f[:-2]) * np.float32(0.5)
+    dy[0], dy[-1] = f[1] - f[0], f[-1] - f[-2]
+    m = np.sqrt(dx * dx + dy * dy, dtype=np.float32)
+    want = np.clip(np.floor(m) + ((m - np.floor(m)) >= 0.5), 0, 255).astype(np.uint8)
+    assert np.array_equal(orc.gradient(img), want)
+
+
+def test_features_count_form_matches_reference_order(orc):
+    """The GPU sums perimeter cell classes as counts; on random discs that
+    equals the reference's ordered double sum to within float rounding."""
+    from nscale_gb300 import synth
+    m = synth.disc_mask(200, 240, seed=77)
+    lab = orc.bwlabel2(m, 8)
+    gray = synth.he_tile(200, 240, seed=78)[:, :, 0]
+    f = orc.nucleus_features(lab, gray)
+    assert len(f) >= 2
+    # count form over the whole image, per component
+    cls = np.zeros(16, int)
+    cls[[1, 2, 4, 8, 7, 11, 13, 14]] = 1
+    cls[[3, 6, 9, 12]] = 2
+    cls[[5, 10]] = 3
+    pad = np.pad(lab, 1, constant_values=-1)
+    roots = np.unique(lab[lab >= 0])
+    for k, L in enumerate(roots):
+        b = (pad == L).astype(int)
+        mk = (b[:-1, :-1] << 3) | (b[:-1, 1:] << 2) | (b[1:, 1:] << 1) | b[1:, :-1]
+        c = cls[mk]
+        per = (c == 1).sum() * 0.70710678118 + (c == 2).sum() * 1.0 + (c == 3).sum() * 1.41421356237
+        assert abs(per - f[k, 1]) <= 1e-5 * max(1.0, per)
+        assert f[k, 0] == (lab == L).sum()
