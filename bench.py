@@ -386,13 +386,19 @@ def pool_workers(args):
 
 def serve(args, tiles, batched_mpx_s):
     """Poisson arrivals of host tiles into nsg_server at `serve_load` x the
-    batched throughput; returns latency percentiles (submit -> result)."""
+    batched throughput, every fifth tile tissue-free (near-white: the
+    BACKGROUND early exit), each result carrying the per-nucleus features of
+    its H channel; returns latency percentiles (submit -> result)."""
     import numpy as np
     import random
-    from nscale_gb300 import _lib
+    from nscale_gb300 import _lib, synth
     from nscale_gb300.serving import TileServer
     sub = tiles[: args.serve_tiles]
-    host = [t.cpu().numpy() for t in sub]
+    mr = max(t.shape[0] for t in sub)
+    mc = max(t.shape[1] for t in sub)
+    white = synth.white_tile(mr, mc, 0x5EED0004)  # cut to each tile's shape
+    host = [t.cpu().numpy() if i % 5 != 4 else np.ascontiguousarray(white[: t.shape[0], : t.shape[1]])
+            for i, t in enumerate(sub)]
     labs = [np.empty(h.shape[:2], np.int32) for h in host]
     maxr = max(h.shape[0] for h in host)
     maxc = max(h.shape[1] for h in host)
@@ -409,14 +415,20 @@ def serve(args, tiles, batched_mpx_s):
         while time.perf_counter() < due:
             results += srv.poll(64, 0)
             time.sleep(min(0.0005, max(0.0, due - time.perf_counter())))
-        srv.submit(h, lab)
+        srv.submit(h, lab, want_features=True)
     while len(results) < len(host):
         results += srv.poll(64, 100)
     wall = time.perf_counter() - t0
     workers = srv.workers
     srv.close()
     lat = sorted(r["latency_ms"] for r in results)
+    st = {}
+    for r in results:
+        st[str(r["status"])] = st.get(str(r["status"]), 0) + 1
+    nfeat = sum(len(r["features"]) for r in results if r["features"] is not None)
     return {"tiles": len(host), "arrivals": "poisson", "offered_tiles_per_s": round(rate, 2),
+            "statuses": st, "nuclei_with_features": nfeat,
+            "output": "labels + per-nucleus area, perimeter, mean/std H, mean gradient",
             "load": args.serve_load, "workers": workers,
             "p50_ms": round(lat[len(lat) // 2], 3), "p99_ms": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3),
             "achieved_tiles_per_s": round(len(host) / wall, 2)}

@@ -248,10 +248,12 @@ typedef struct nsg_tile {
     int32_t *labels;         /* nullable output (same memory kind as bgr) */
     uint8_t *mask;           /* nullable output (same memory kind as bgr) */
     int want_bbox;           /* 1: fill bbox (nsg_alloc'd, free with nsg_free) */
+    int want_features;       /* 1: per-nucleus features of the H channel (nsg_nucleus_features) */
     /* results */
     int status;              /* segmentNuclei status or NSG_ERR_* */
     int compcount;
     int32_t *bbox;
+    float *features;         /* compcount x NSG_N_FEATURES, nsg_alloc'd (free with nsg_free), or NULL */
 } nsg_tile;
 #define NSG_TILE_HOST 1 /* flag: bgr / labels / mask are host pointers */
 
@@ -277,6 +279,7 @@ typedef struct nsg_result {
     long long ticket;
     int status, compcount;
     int32_t *bbox;           /* when the tile asked for it: nsg_alloc'd, free with nsg_free */
+    float *features;         /* when the tile asked for it: compcount x NSG_N_FEATURES, nsg_alloc'd */
     double latency_ms;       /* submit -> result ready */
 } nsg_result;
 size_t nsg_pool_context_bytes(int max_rows, int max_cols);

@@ -47,15 +47,16 @@ class Tile(C.Structure):
     """nsg_tile: one tile of a batch or server submission (include/nsg.h)."""
 
     _fields_ = [("bgr", C.c_void_p), ("rows", C.c_int), ("cols", C.c_int), ("row_stride_bytes", C.c_size_t),
-                ("labels", C.c_void_p), ("mask", C.c_void_p), ("want_bbox", C.c_int),
-                ("status", C.c_int), ("compcount", C.c_int), ("bbox", C.POINTER(C.c_int32))]
+                ("labels", C.c_void_p), ("mask", C.c_void_p), ("want_bbox", C.c_int), ("want_features", C.c_int),
+                ("status", C.c_int), ("compcount", C.c_int), ("bbox", C.POINTER(C.c_int32)),
+                ("features", C.POINTER(C.c_float))]
 
 
 class Result(C.Structure):
     """nsg_result: one finished server tile."""
 
     _fields_ = [("ticket", C.c_longlong), ("status", C.c_int), ("compcount", C.c_int),
-                ("bbox", C.POINTER(C.c_int32)), ("latency_ms", C.c_double)]
+                ("bbox", C.POINTER(C.c_int32)), ("features", C.POINTER(C.c_float)), ("latency_ms", C.c_double)]
 
 
 TILE_HOST = 1

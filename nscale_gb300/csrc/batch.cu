@@ -43,19 +43,78 @@ struct Worker {
     std::thread th;
 };
 
+// H channel (colour deconvolution with the feature pipeline's stains) and
+// the per-nucleus features of a segmented tile, copied to an nsg_alloc'd
+// host array.  Scratch: p_u8[0] (H), p_f32[0] (features), and the feature
+// pass's own planes; the labels must live elsewhere.
+int tile_features(nsg::Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int cols, const int32_t *lab,
+                  nsg_tile &t, cudaStream_t s) {
+    float q[6];
+    if (nsg_stain_matrix(nullptr, nullptr, q) != NSG_SUCCESS) return NSG_ERR_ARG;
+    uint8_t *H = c.ws.p_u8[0];
+    float *fd = c.ws.p_f32[0];
+    NSG_TRY(nsg::color_deconv_dev(c, bgr, stride, rows, cols, q, H, nullptr, s));
+    int cnt = 0;
+    const int cap = (int)std::min<int64_t>(c.max_pad / NSG_N_FEATURES, 1 << 30);
+    NSG_TRY(nsg::nucleus_features_dev(c, lab, H, rows, cols, fd, cap, &cnt, s));
+    float *fh = (float *)nsg_alloc(sizeof(float) * NSG_N_FEATURES * (size_t)(cnt > 0 ? cnt : 1));
+    if (!fh) return NSG_ERR_OOM;
+    if (cnt > 0) {
+        cudaError_t e = cudaMemcpyAsync(fh, fd, sizeof(float) * NSG_N_FEATURES * (size_t)cnt, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            nsg_free(fh);
+            return NSG_ERR_CUDA;
+        }
+    }
+    t.features = fh;
+    return NSG_SUCCESS;
+}
+
 // one tile through the pipeline on a worker; outputs are complete on return
 void run_tile(nsg_context *ctx, cudaStream_t s, nsg_tile &t, const nsg_seg_params &p, bool host) {
     t.compcount = 0;
     t.bbox = nullptr;
+    t.features = nullptr;
     int32_t **bb = t.want_bbox ? &t.bbox : nullptr;
     int st;
-    if (host) {
-        st = nsg_segment_nuclei_host(ctx, t.bgr, t.rows, t.cols, &p, t.labels, t.mask, &t.compcount, bb, s);
-    } else {
-        const size_t stride = t.row_stride_bytes ? t.row_stride_bytes : (size_t)t.cols * 3;
-        st = nsg_segment_nuclei(ctx, t.bgr, t.rows, t.cols, stride, &p, t.labels, t.mask, &t.compcount, bb, s);
-        if (cudaStreamSynchronize(s) != cudaSuccess && st >= 0) st = NSG_ERR_CUDA;
+    if (!t.want_features) {
+        if (host) {
+            st = nsg_segment_nuclei_host(ctx, t.bgr, t.rows, t.cols, &p, t.labels, t.mask, &t.compcount, bb, s);
+        } else {
+            const size_t stride = t.row_stride_bytes ? t.row_stride_bytes : (size_t)t.cols * 3;
+            st = nsg_segment_nuclei(ctx, t.bgr, t.rows, t.cols, stride, &p, t.labels, t.mask, &t.compcount, bb, s);
+            if (cudaStreamSynchronize(s) != cudaSuccess && st >= 0) st = NSG_ERR_CUDA;
+        }
+        t.status = st;
+        return;
     }
+    // with features: the pipeline on device buffers, then the feature pass
+    nsg::Ctx &c = ctx->c;
+    if (!t.bgr || t.rows <= 0 || t.cols <= 0 || (int64_t)t.rows * t.cols > c.max_px) {
+        t.status = t.bgr ? NSG_ERR_ARG : NSG_INVALID_IMAGE;
+        return;
+    }
+    const int64_t n = (int64_t)t.rows * t.cols;
+    const uint8_t *bgr = t.bgr;
+    int64_t stride = t.row_stride_bytes ? (int64_t)t.row_stride_bytes : (int64_t)t.cols * 3;
+    int32_t *lab = host ? (int32_t *)c.ws.i32[5] : (t.labels ? t.labels : c.ws.p_i32[0]);
+    uint8_t *msk = t.mask ? (host ? c.ws.p_u8[9] : t.mask) : nullptr;
+    if (host) {
+        if (cudaMemcpyAsync(c.ws.p_bgr, t.bgr, (size_t)n * 3, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+            t.status = NSG_ERR_CUDA;
+            return;
+        }
+        bgr = c.ws.p_bgr;
+        stride = (int64_t)t.cols * 3;
+    }
+    st = nsg::segment_nuclei_dev(c, bgr, stride, t.rows, t.cols, p, lab, msk, &t.compcount, bb, s);
+    if (st == NSG_SUCCESS) st = tile_features(c, bgr, stride, t.rows, t.cols, lab, t, s);
+    if (st >= 0 && host) {
+        if (t.labels) cudaMemcpyAsync(t.labels, lab, (size_t)n * 4, cudaMemcpyDeviceToHost, s);
+        if (t.mask) cudaMemcpyAsync(t.mask, msk, (size_t)n, cudaMemcpyDeviceToHost, s);
+    }
+    if (cudaStreamSynchronize(s) != cudaSuccess && st >= 0) st = NSG_ERR_CUDA;
     t.status = st;
 }
 
@@ -100,6 +159,7 @@ struct nsg_pool {
                 r.status = j.tile.status;
                 r.compcount = j.tile.compcount;
                 r.bbox = j.tile.bbox;
+                r.features = j.tile.features;
                 r.latency_ms = std::chrono::duration<double, std::milli>(Clock::now() - j.t_submit).count();
                 lk.lock();
                 done.push_back(r);

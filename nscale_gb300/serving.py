@@ -22,6 +22,14 @@ def _check(rc: int, what: str) -> None:
         raise _lib.NsgError(rc, what)
 
 
+def _feature_array(L, ptr, n: int) -> np.ndarray | None:
+    if not ptr:
+        return None
+    arr = np.ctypeslib.as_array(ptr, shape=(5 * n,)).copy().reshape(n, 5) if n else np.zeros((0, 5), np.float32)
+    L.nsg_free(ptr)
+    return arr
+
+
 def _bbox_array(L, ptr, n: int) -> np.ndarray:
     if not ptr:
         return np.zeros((5, 0), np.int32)
@@ -51,9 +59,12 @@ class TilePool:
         _check(rc, "nsg_segment_nuclei_batch")
         return rc
 
-    def segment(self, images, params: _lib.SegParams | None = None, want_bbox: bool = True):
+    def segment(self, images, params: _lib.SegParams | None = None, want_bbox: bool = True,
+                want_features: bool = False):
         """segmentNuclei on every image (BGR uint8 (rows, cols, 3) CUDA tensors,
-        or host numpy arrays).  Returns [(status, labels, compcount, bbox)]."""
+        or host numpy arrays).  Returns [(status, labels, compcount, bbox)], with
+        a fifth element, the (n, 5) per-nucleus features of the H channel
+        (area, perimeter, mean H, std H, mean gradient), when want_features."""
         host = not isinstance(images[0], torch.Tensor) or not images[0].is_cuda
         arr = (_lib.Tile * len(images))()
         keep = []
@@ -70,11 +81,15 @@ class TilePool:
             arr[i].bgr, arr[i].rows, arr[i].cols = bgr_p, im.shape[0], im.shape[1]
             arr[i].row_stride_bytes = 0
             arr[i].labels, arr[i].mask, arr[i].want_bbox = lab_p, None, 1 if want_bbox else 0
+            arr[i].want_features = 1 if want_features else 0
         self.run(arr, params, host)
         out = []
         for i, (im, lab) in enumerate(keep):
             t = arr[i]
-            out.append((t.status, lab, t.compcount, _bbox_array(self.L, t.bbox, t.compcount)))
+            r = (t.status, lab, t.compcount, _bbox_array(self.L, t.bbox, t.compcount))
+            if want_features:
+                r = r + (_feature_array(self.L, t.features, t.compcount),)
+            out.append(r)
         return out
 
     def close(self) -> None:
@@ -108,14 +123,14 @@ class TileServer:
         return self.L.nsg_server_workers(self.h)
 
     def submit(self, image: np.ndarray, labels: np.ndarray | None = None, want_bbox: bool = False,
-               params: _lib.SegParams | None = None) -> int:
+               params: _lib.SegParams | None = None, want_features: bool = False) -> int:
         """Queue one host BGR tile; `labels` (int32, rows x cols) receives the
         label image.  Both arrays stay referenced until the result is polled."""
         image = np.ascontiguousarray(image, dtype=np.uint8)
         t = _lib.Tile()
         t.bgr, t.rows, t.cols, t.row_stride_bytes = image.ctypes.data, image.shape[0], image.shape[1], 0
         t.labels = labels.ctypes.data if labels is not None else None
-        t.mask, t.want_bbox = None, 1 if want_bbox else 0
+        t.mask, t.want_bbox, t.want_features = None, 1 if want_bbox else 0, 1 if want_features else 0
         ticket = C.c_longlong(-1)
         _check(self.L.nsg_server_submit(self.h, C.byref(t), C.byref(params) if params else None, C.byref(ticket)),
                "nsg_server_submit")
@@ -132,6 +147,7 @@ class TileServer:
             _, labels = self._live.pop(r.ticket, (None, None))
             out.append({"ticket": r.ticket, "status": r.status, "compcount": r.compcount,
                         "bbox": _bbox_array(self.L, r.bbox, r.compcount), "labels": labels,
+                        "features": _feature_array(self.L, r.features, r.compcount),
                         "latency_ms": r.latency_ms})
         return out
 

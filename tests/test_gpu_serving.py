@@ -108,3 +108,32 @@ def test_server_queue_bound(cuda):
         assert all(r["status"] == 0 for r in got)
     finally:
         srv.close()
+
+
+def test_server_features_match_feature_entry(cuda):
+    """A tile served with want_features gets the features nsg_nucleus_features
+    computes from its labels and the H channel of nsg_color_deconv."""
+    import torch
+    from nscale_gb300 import _lib, synth
+    from nscale_gb300.features import ObjFeatures
+    from nscale_gb300.histological_entities import PixelOperations as PO
+    from nscale_gb300.serving import TilePool, TileServer
+    img = synth.he_tile(700, 900, seed=0x5EED7300)
+    per = _lib.load().nsg_pool_context_bytes(700, 900)
+    srv = TileServer(700, 900, 2 * per, queue_cap=4)
+    try:
+        lab = np.empty(img.shape[:2], np.int32)
+        srv.submit(img, lab, want_features=True)
+        (r,) = srv.poll(1, 60000)
+    finally:
+        srv.close()
+    assert r["status"] == 0 and r["compcount"] > 0
+    H, _ = PO.ColorDeconv(torch.from_numpy(img).cuda())
+    want = ObjFeatures.nucleusFeatures(torch.from_numpy(lab).cuda(), H).cpu().numpy()
+    assert np.array_equal(r["features"], want)
+    pool = TilePool(700, 900, workers=2)
+    try:
+        (st, lab2, n, bb, feats), = pool.segment([torch.from_numpy(img).cuda()], want_features=True)
+    finally:
+        pool.close()
+    assert st == 0 and np.array_equal(lab2.cpu().numpy(), lab) and np.array_equal(feats, want)
