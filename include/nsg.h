@@ -174,8 +174,8 @@ int nsg_watershed_serial(nsg_context *ctx, const uint8_t *bgr, const float *img,
  * [2] background entries recorded, [6] level of the first background pop,
  * [9] 1 if a background flood event happened, [11] BFS layers; and of the
  * last grey reconstruction: [12] tile passes, [13] in-tile row+column
- * sweeps, [15] pixels changed by its whole-image sweeps; [14] CTAs in the
- * BFS cluster. */
+ * sweeps, [15] tile lines (rows + columns) scanned; [14] CTAs in the BFS
+ * cluster. */
 int nsg_watershed_diagnostics(nsg_context *ctx, int *out16, nsg_stream_t stream);
 /* ConnComponents::boundingBox (ConnComponents.cpp:241-284) on a -1-background
  * label image: writes compcount entries of (label, minx, maxx, miny, maxy) as

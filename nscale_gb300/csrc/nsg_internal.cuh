@@ -62,7 +62,7 @@ enum Ctrl : int {
     C_QPEND = 10,
     C_FLAG0 = 16,
     C_FLAG1 = 17,
-    C_RSTATS = 20,   // grey reconstruction: tile passes, sweeps, pixels changed by whole-image sweeps
+    C_RSTATS = 20,   // grey reconstruction: tile passes, sweeps, pixels changed by whole-image sweeps, lines scanned
     C_WS = 64,       // watershed control block (64 ints)
     C_QSLOTS = 1024, // 3072 ints: generic small arrays
 };

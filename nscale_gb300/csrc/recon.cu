@@ -108,6 +108,7 @@ __global__ void init_queue(int *state, int *queue, int *dirty, int qcap, int nti
         ctrl[C_QPEND] = ntiles;
         ctrl[C_RSTATS] = 0;
         ctrl[C_RSTATS + 1] = 0;
+        ctrl[C_RSTATS + 3] = 0;
     }
 }
 
@@ -254,6 +255,7 @@ __global__ void __launch_bounds__(1024) queue_marked(int *state, int *queue, con
         ctrl[C_QPEND] = carry;
         ctrl[C_RSTATS] = 0;
         ctrl[C_RSTATS + 1] = 0;
+        ctrl[C_RSTATS + 3] = 0;
     }
 }
 
@@ -351,7 +353,7 @@ struct TileSmem {
     T eN[TW], eS[TW], eW[TH], eE[TH];          // the tile's edge values when it was loaded
     T mN[TW + 2], mS[TW + 2], mW[TH], mE[TH];  // the mask just outside the tile (neighbours' pixels)
     unsigned drow[TH / 32], dcol[TW / 32];     // dirty rows / columns
-    int edges, tile, again, sweeps, dirty;
+    int edges, tile, again, sweeps, dirty, lines;
 };
 
 // Whole warp: lane l changed the pixels of its K-pixel slice (l*K .. l*K+K-1)
@@ -488,6 +490,7 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
     if (threadIdx.x == 0) {
         sm.edges = 0;
         sm.sweeps = 0;
+        sm.lines = 0;
     }
     __syncthreads();
     for (int i = threadIdx.x; i < TW; i += NW * 32) {
@@ -506,6 +509,8 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
         unsigned rm[TH / 32];
 #pragma unroll
         for (int w = 0; w < TH / 32; ++w) rm[w] = sm.drow[w];
+        if (threadIdx.x == 0)
+            for (int w = 0; w < TH / 32; ++w) sm.lines += __popc(rm[w]);
         __syncthreads();
         if (threadIdx.x < TH / 32) sm.drow[threadIdx.x] = 0;
         bool chr = false;
@@ -552,6 +557,8 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
         unsigned cm[TW / 32];
 #pragma unroll
         for (int w = 0; w < TW / 32; ++w) cm[w] = sm.dcol[w];
+        if (threadIdx.x == 0)
+            for (int w = 0; w < TW / 32; ++w) sm.lines += __popc(cm[w]);
         __syncthreads();
         if (threadIdx.x < TW / 32) sm.dcol[threadIdx.x] = 0;
         bool chc = false;
@@ -703,6 +710,7 @@ __global__ void __launch_bounds__(NW * 32, NW >= 16 ? 1 : 2) recon_cta(const T *
                 if (edges & 256u && ty + 1 < tiles_y && tx + 1 < tiles_x) notify(q, t + tiles_x + 1, D_N);
                 atomicAdd(q.stats, 1);
                 atomicAdd(q.stats + 1, sm.sweeps);
+                atomicAdd(q.stats + 3, sm.lines);
                 sm.again = q_finish(q, t);
             }
             __syncthreads();

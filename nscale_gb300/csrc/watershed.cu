@@ -107,7 +107,7 @@ int watershed_diag(Ctx &c, int *out16, cudaStream_t s) {
     NSG_CUDA_TRY(c, cudaMemcpyAsync(c.ws.h_ctrl, c.ws.ctrl + C_WS, 13 * sizeof(int), cudaMemcpyDeviceToHost, s));
     NSG_CUDA_TRY(c, cudaMemcpyAsync(c.ws.h_ctrl + 14, c.ws.ctrl + C_WS + 12, sizeof(int), cudaMemcpyDeviceToHost, s));
     NSG_CUDA_TRY(c, cudaMemcpyAsync(c.ws.h_ctrl + 12, c.ws.ctrl + C_RSTATS, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
-    NSG_CUDA_TRY(c, cudaMemcpyAsync(c.ws.h_ctrl + 15, c.ws.ctrl + C_RSTATS + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NSG_CUDA_TRY(c, cudaMemcpyAsync(c.ws.h_ctrl + 15, c.ws.ctrl + C_RSTATS + 3, sizeof(int), cudaMemcpyDeviceToHost, s));
     NSG_CUDA_TRY(c, cudaStreamSynchronize(s));
     for (int i = 0; i < 16; ++i) out16[i] = c.ws.h_ctrl[i];
     return NSG_SUCCESS;

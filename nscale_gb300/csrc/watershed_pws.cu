@@ -576,8 +576,8 @@ __global__ void k_bfs_prep(PW a, uint8_t *nbm) {
 // contiguous chunks, one per CTA, staged in shared memory; after the claims a cluster
 // barrier, then each CTA compacts its winners in order into its own segment
 // of the next frontier and publishes their count in shared memory; after a
-// second barrier every CTA reads all counts (distributed shared memory) to
-// place the segments.  Chunks are contiguous and ordered by CTA, so the next
+// second barrier every CTA reads all counts (each CTA pushed its count into
+// every CTA's shared memory) to place the segments.  Chunks are contiguous and ordered by CTA, so the next
 // frontier in global order is the concatenation of the segments.
 constexpr int kBfsThreads = 256, kBfsCtaItems = 4096, kBfsMaxCluster = 16;
 constexpr int kBfsPerThread = kBfsCtaItems / kBfsThreads;  // <= 16: 64 claim bits per thread
@@ -587,25 +587,29 @@ __global__ void __launch_bounds__(kBfsThreads) k_bfs(PW a, const uint8_t *__rest
     cg::cluster_group cl = cg::this_cluster();
     const int C = (int)cl.num_blocks(), me = (int)cl.block_rank();
     __shared__ int sh[40];
-    __shared__ int tot;                      // winners of this CTA in the last layer
+    __shared__ int tots[kBfsMaxCluster];      // winners of every CTA in the last layer (pushed by each CTA)
     __shared__ int offs[kBfsMaxCluster + 1];  // where each CTA's segment starts in global order
     __shared__ int s_r[kBfsCtaItems];         // this CTA's chunk of the frontier
     __shared__ uint8_t s_m[kBfsCtaItems];     // and the chunk's neighbour classes
+    __shared__ uint8_t s_nm[kBfsCtaItems * 4];  // neighbour classes of the pixels this CTA wins
     const bool on = a.ctl[W_EVENT] && !a.ctl[W_FALLBACK];
     const int W = a.W;
-    int *Fc = a.fr0, *Fn = a.fr1;
-    if (threadIdx.x == 0) {
-        tot = me == 0 ? 1 : 0;
-        if (me == 0 && on) Fc[0] = a.ctl[W_EP];
+    // frontier entries carry their pixel's neighbour classes (one load less per layer)
+    unsigned long long *Fc = reinterpret_cast<unsigned long long *>(a.fr0);
+    unsigned long long *Fn = reinterpret_cast<unsigned long long *>(a.fr1);
+    if (threadIdx.x < kBfsMaxCluster) tots[threadIdx.x] = threadIdx.x == 0 ? 1 : 0;
+    if (threadIdx.x == 0 && me == 0 && on) {
+        const int ep = a.ctl[W_EP];
+        Fc[0] = (unsigned)ep | ((unsigned long long)nbm[ep] << 32);
     }
     cl.sync();  // every CTA has read the control flags before anything can change them
     if (!on) return;
     const int off[4] = {-1, 1, -W, W};
     int prevcap = 1, base = 0, layer = 0;
     for (;;) {
-        if (threadIdx.x < 32) {  // every CTA's count, read in parallel, then a warp scan
+        if (threadIdx.x < 32) {  // every CTA's count (local copies), then a warp scan
             const int lane = threadIdx.x;
-            const int v = lane < C ? *cl.map_shared_rank(&tot, lane) : 0;
+            const int v = lane < C ? tots[lane] : 0;
             int x = v;
 #pragma unroll
             for (int d = 1; d < 32; d <<= 1) {
@@ -628,9 +632,9 @@ __global__ void __launch_bounds__(kBfsThreads) k_bfs(PW a, const uint8_t *__rest
         int seg = 0;
         for (int i = lo + threadIdx.x; i < hi; i += kBfsThreads) {
             while (i >= offs[seg + 1]) ++seg;
-            const int r = __ldcg(Fc + seg * prevcap + (i - offs[seg]));
-            s_r[i - lo] = r;
-            s_m[i - lo] = nbm[r];
+            const unsigned long long e = __ldcg(Fc + seg * prevcap + (i - offs[seg]));
+            s_r[i - lo] = (int)(unsigned)e;
+            s_m[i - lo] = (uint8_t)(e >> 32);
         }
         __syncthreads();
         const int pt = (cnt + kBfsThreads - 1) / kBfsThreads;
@@ -651,9 +655,19 @@ __global__ void __launch_bounds__(kBfsThreads) k_bfs(PW a, const uint8_t *__rest
             const int r = s_r[j0 + j];
             const unsigned m = s_m[j0 + j];
             const int key0 = (base + lo + j0 + j) * 4;
+            int cl4[4];
+            uint8_t nm4[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {  // both loads of every candidate issued together
+                cl4[k] = (m & (1u << k)) ? __ldcg(a.claim + r + off[k]) : -1;
+                nm4[k] = (m & (1u << k)) ? nbm[r + off[k]] : 0;
+            }
 #pragma unroll
             for (int k = 0; k < 4; ++k)
-                if ((m & (1u << k)) && __ldcg(a.claim + r + off[k]) == key0 + k) win |= 1ull << (j * 4 + k);
+                if ((m & (1u << k)) && cl4[k] == key0 + k) {
+                    win |= 1ull << (j * 4 + k);
+                    s_nm[(j0 + j) * 4 + k] = nm4[k];
+                }
         }
         int total;
         int pos = cta_exclusive_scan(__popcll(win), sh, total);
@@ -661,12 +675,12 @@ __global__ void __launch_bounds__(kBfsThreads) k_bfs(PW a, const uint8_t *__rest
             const int b = __ffsll((long long)win) - 1;
             win &= win - 1;
             const int q = s_r[j0 + (b >> 2)] + off[b & 3];
-            Fn[me * segcap + pos] = q;
+            Fn[me * segcap + pos] = (unsigned)q | ((unsigned long long)s_nm[j0 * 4 + b] << 32);
             a.st[q] |= S_R;
             ++pos;
         }
-        if (threadIdx.x == 0) tot = total;
-        int *t = Fc;
+        if (threadIdx.x < C) *cl.map_shared_rank(&tots[me], threadIdx.x) = total;  // push the count to all
+        unsigned long long *t = Fc;
         Fc = Fn;
         Fn = t;
         prevcap = segcap;
@@ -1219,8 +1233,8 @@ void carve(PW &a, char *base, size_t *used_out) {
     a.claim = cv.take<int>(n);
     a.uown = cv.take<int>(n);
     a.proot = cv.take<int>(n);
-    a.fr0 = cv.take<int>(n);
-    a.fr1 = cv.take<int>(n);
+    a.fr0 = cv.take<int>(2 * n);  // BFS frontier entries: pixel | neighbour classes << 32
+    a.fr1 = cv.take<int>(2 * n);
     a.popl = cv.take<int>(n);
     a.isroot = cv.take<int>(n);
     a.rank = cv.take<int>(n);
