@@ -30,6 +30,8 @@
 #include <math.h>
 #include <stdlib.h>
 
+#include <type_traits>
+
 #include "nsg_internal.cuh"
 
 namespace nsg {
@@ -671,17 +673,322 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
     __syncthreads();
 }
 
+// ---- packed uint8 tile pass ---------------------------------------------------
+// The uint8 reconstruction keeps its tile twice in shared memory, row-major
+// (`o`) and transposed (`oT`), so that both phases are the same "strip" scan:
+// a warp takes 4 adjacent lines as one 32-bit word per position and scans
+// across the lanes with byte-wise SIMD (__vmaxu4 / __vminu4), 4 lines per
+// instruction.  The row phase is a strip scan on oT, the column phase one on
+// o; a phase writes the words it changes into its own layout and the changed
+// bytes into the other one.  Interior pixel (r, c) of a layout with pitch PL
+// sits at byte (r + 1) * PL + 4 + c, so every strip word is 4-byte aligned
+// and its halo neighbours are byte 3 of the word before / byte 0 of the word
+// after.
+template <int TW, int TH>
+struct TileU8 {
+    static constexpr int P = TW + 8;   // pitch of o: 4 pad bytes, halo at byte 3, TW pixels, halo, pad
+    static constexpr int PT = TH + 8;  // pitch of oT
+    uint8_t o[(TH + 2) * P];
+    uint8_t oT[(TW + 2) * PT];
+    uint8_t m[TH * TW];   // mask, row-major
+    uint8_t mT[TW * TH];  // mask, transposed
+    uint8_t eN[TW], eS[TW], eW[TH], eE[TH];
+    uint8_t mN[TW + 2], mS[TW + 2], mW[TH], mE[TH];
+    unsigned drow[TH / 32], dcol[TW / 32];
+    int edges, tile, again, sweeps, dirty, lines;
+};
+
+__device__ __forceinline__ uint32_t clamp4(uint32_t x, uint32_t lo, uint32_t hi) {
+    return __vminu4(__vmaxu4(x, lo), hi);
+}
+
+// forward then backward clamp scans of K words per lane (4 lines at once)
+template <int K>
+__device__ __forceinline__ void line_scan_u8x4(const uint32_t (&lo)[K], const uint32_t (&hi)[K], uint32_t first,
+                                               uint32_t last, uint32_t (&res)[K]) {
+    const int lane = threadIdx.x & 31;
+    uint32_t FL = lo[0], FH = hi[0];
+#pragma unroll
+    for (int k = 1; k < K; ++k) {
+        const uint32_t nl = clamp4(FL, lo[k], hi[k]), nh = clamp4(FH, lo[k], hi[k]);
+        FL = nl;
+        FH = nh;
+    }
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t pl = __shfl_up_sync(0xffffffffu, FL, d), ph = __shfl_up_sync(0xffffffffu, FH, d);
+        if (lane >= d) {
+            const uint32_t nl = clamp4(pl, FL, FH), nh = clamp4(ph, FL, FH);
+            FL = nl;
+            FH = nh;
+        }
+    }
+    uint32_t el = __shfl_up_sync(0xffffffffu, FL, 1), eh = __shfl_up_sync(0xffffffffu, FH, 1);
+    uint32_t y = lane == 0 ? first : clamp4(first, el, eh);
+    uint32_t v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        y = clamp4(y, lo[k], hi[k]);
+        v[k] = y;
+    }
+    // backward on the forward result: g_k(y) = clamp(y, v_k, hi_k) (v_k <= hi_k)
+    uint32_t BL = v[K - 1], BH = hi[K - 1];
+#pragma unroll
+    for (int k = K - 2; k >= 0; --k) {
+        const uint32_t nl = clamp4(BL, v[k], hi[k]), nh = clamp4(BH, v[k], hi[k]);
+        BL = nl;
+        BH = nh;
+    }
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t pl = __shfl_down_sync(0xffffffffu, BL, d), ph = __shfl_down_sync(0xffffffffu, BH, d);
+        if (lane + d < 32) {
+            const uint32_t nl = clamp4(pl, BL, BH), nh = clamp4(ph, BL, BH);
+            BL = nl;
+            BH = nh;
+        }
+    }
+    el = __shfl_down_sync(0xffffffffu, BL, 1);
+    eh = __shfl_down_sync(0xffffffffu, BH, 1);
+    y = lane == 31 ? last : clamp4(last, el, eh);
+#pragma unroll
+    for (int k = K - 1; k >= 0; --k) {
+        y = clamp4(y, v[k], hi[k]);
+        res[k] = y;
+    }
+}
+
+// One phase on layout L (LEN interior rows, the scan direction; NL interior
+// columns, the lines): every dirty strip of 4 columns is scanned down and up.
+// Changed words are stored into L, changed bytes into X (the transpose, pitch
+// PX), and rows next to a change are marked in `other` (LEN bits).  Returns
+// whether this warp changed anything.
+template <int LEN, int NL, int PL, int PX, int NW>
+__device__ bool strip_phase(uint8_t *L, const uint8_t *__restrict__ M, uint8_t *X, const unsigned (&dirty)[NL / 32],
+                            unsigned *other, bool conn8, int &lines) {
+    constexpr int K = LEN / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    bool ch = false;
+    int seq = 0;
+#pragma unroll
+    for (int w = 0; w < NL / 32; ++w) {
+#pragma unroll 1
+        for (int g = 0; g < 8; ++g) {  // 8 strips of 4 columns per 32-bit dirty word
+            if (!((dirty[w] >> (4 * g)) & 15u)) continue;
+            if ((seq++ & (NW - 1)) != warp) continue;
+            if (lane == 0) ++lines;
+            const int s = w * 8 + g;
+            const int cb = 4 + 4 * s;
+            uint32_t cur[K], h2[K + 2];
+#pragma unroll
+            for (int t = 0; t < K + 2; ++t) {
+                const uint8_t *row = L + (lane * K + t) * PL;  // L-row lane*K - 1 + t
+                const uint32_t c = *reinterpret_cast<const uint32_t *>(row + cb);
+                const uint32_t l = *reinterpret_cast<const uint32_t *>(row + cb - 4);
+                const uint32_t r = *reinterpret_cast<const uint32_t *>(row + cb + 4);
+                h2[t] = __vmaxu4(__byte_perm(l, c, 0x6543), __byte_perm(c, r, 0x4321));
+                if (t >= 1 && t <= K) cur[t - 1] = c;
+            }
+            uint32_t lo[K], hi[K], res[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const uint32_t mk = *reinterpret_cast<const uint32_t *>(M + (lane * K + k) * NL + 4 * s);
+                uint32_t w8 = __vmaxu4(cur[k], h2[k + 1]);
+                if (conn8) w8 = __vmaxu4(w8, __vmaxu4(h2[k], h2[k + 2]));
+                lo[k] = __vminu4(w8, mk);
+                hi[k] = mk;
+            }
+            const uint32_t first = *reinterpret_cast<const uint32_t *>(L + cb);
+            const uint32_t last = *reinterpret_cast<const uint32_t *>(L + (LEN + 1) * PL + cb);
+            line_scan_u8x4<K>(lo, hi, first, last, res);
+            unsigned changed = 0;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const uint32_t diff = res[k] ^ cur[k];
+                if (diff) {
+                    const int r = lane * K + k;
+                    *reinterpret_cast<uint32_t *>(L + (r + 1) * PL + cb) = res[k];
+#pragma unroll
+                    for (int b = 0; b < 4; ++b)
+                        if ((diff >> (8 * b)) & 255u) X[(4 * s + b + 1) * PX + 4 + r] = (uint8_t)(res[k] >> (8 * b));
+                    changed |= 1u << k;
+                }
+            }
+            if (__any_sync(0xffffffffu, changed != 0)) {
+                ch = true;
+                mark_dirty<K, LEN>(other, changed);
+            }
+        }
+    }
+    return ch;
+}
+
+template <int TW, int TH, int NW>
+__device__ void cta_process_tile_u8(const uint8_t *__restrict__ mask, uint8_t *out, int rows, int cols, bool conn8,
+                                    int tx, int ty, int dirty_in, TileU8<TW, TH> &sm) {
+    constexpr int P = TileU8<TW, TH>::P, PT = TileU8<TW, TH>::PT;
+    const int y0 = ty * TH, x0 = tx * TW;
+    uint8_t *o = sm.o, *oT = sm.oT;
+    auto O = [&](int y, int x) -> uint8_t & { return o[(y + 1) * P + 4 + x]; };  // y in [-1, TH], x in [-1, TW]
+    // load tile + halo (image ring = 0) into both layouts, and the mask
+    for (int i = threadIdx.x; i < (TH + 2) * (TW + 2); i += NW * 32) {
+        const int r = i / (TW + 2) - 1, cc = i - (r + 1) * (TW + 2) - 1;
+        const int y = y0 + r, x = x0 + cc;
+        const uint8_t v = (y >= 0 && y < rows && x >= 0 && x < cols) ? ldcg(out + (int64_t)y * cols + x) : 0;
+        o[(r + 1) * P + 4 + cc] = v;
+        oT[(cc + 1) * PT + 4 + r] = v;
+    }
+    for (int i = threadIdx.x; i < TH * TW; i += NW * 32) {
+        const int r = i / TW, cc = i - r * TW;
+        const int y = y0 + r, x = x0 + cc;
+        const uint8_t v = (y < rows && x < cols) ? __ldg(mask + (int64_t)y * cols + x) : 0;
+        sm.m[r * TW + cc] = v;
+        sm.mT[cc * TH + r] = v;
+    }
+    auto mask_at = [&](int y, int x) -> uint8_t {
+        return (y >= 0 && y < rows && x >= 0 && x < cols) ? __ldg(mask + (int64_t)y * cols + x) : 0;
+    };
+    for (int i = threadIdx.x; i < TW + 2; i += NW * 32) {
+        sm.mN[i] = mask_at(y0 - 1, x0 - 1 + i);
+        sm.mS[i] = mask_at(y0 + TH, x0 - 1 + i);
+    }
+    for (int i = threadIdx.x; i < TH; i += NW * 32) {
+        sm.mW[i] = mask_at(y0 + i, x0 - 1);
+        sm.mE[i] = mask_at(y0 + i, x0 + TW);
+    }
+    const bool all = dirty_in & D_ALL;
+    if (threadIdx.x < TH / 32) {
+        const int w = threadIdx.x;
+        unsigned b = all ? ~0u : 0u;
+        if ((dirty_in & D_N) && w == 0) b |= 1u;
+        if ((dirty_in & D_S) && w == TH / 32 - 1) b |= 1u << 31;
+        sm.drow[w] = b;
+    }
+    if (threadIdx.x >= 32 && threadIdx.x < 32 + TW / 32) {
+        const int w = threadIdx.x - 32;
+        unsigned b = all ? ~0u : 0u;
+        if ((dirty_in & D_W) && w == 0) b |= 1u;
+        if ((dirty_in & D_E) && w == TW / 32 - 1) b |= 1u << 31;
+        sm.dcol[w] = b;
+    }
+    if (threadIdx.x == 0) {
+        sm.edges = 0;
+        sm.sweeps = 0;
+        sm.lines = 0;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < TW; i += NW * 32) {
+        sm.eN[i] = O(0, i);
+        sm.eS[i] = O(TH - 1, i);
+    }
+    for (int i = threadIdx.x; i < TH; i += NW * 32) {
+        sm.eW[i] = O(i, 0);
+        sm.eE[i] = O(i, TW - 1);
+    }
+    unsigned my_edges = 0;
+    bool anych = false;
+    int lines = 0;
+    for (int it = 0; it < 1024; ++it) {
+        // ---- row phase: strips of 4 rows, scanned along x in the transposed copy
+        unsigned rm[TH / 32];
+#pragma unroll
+        for (int w = 0; w < TH / 32; ++w) rm[w] = sm.drow[w];
+        __syncthreads();
+        if (threadIdx.x < TH / 32) sm.drow[threadIdx.x] = 0;
+        bool chr = strip_phase<TW, TH, PT, P, NW>(oT, sm.mT, o, rm, sm.dcol, conn8, lines);
+        chr = __syncthreads_or(chr);
+        // ---- column phase: strips of 4 columns, scanned along y in the tile
+        unsigned cm[TW / 32];
+#pragma unroll
+        for (int w = 0; w < TW / 32; ++w) cm[w] = sm.dcol[w];
+        __syncthreads();
+        if (threadIdx.x < TW / 32) sm.dcol[threadIdx.x] = 0;
+        bool chc = strip_phase<TH, TW, P, PT, NW>(o, sm.m, oT, cm, sm.drow, conn8, lines);
+        chc = __syncthreads_or(chc);
+        if (threadIdx.x == 0) sm.sweeps = it + 1;
+        anych = anych || chr || chc;
+        if (!chc) break;  // no row is dirty: the tile is stable
+        if (it == 1023) my_edges |= 16u;  // not stable yet: process again later
+    }
+    if ((threadIdx.x & 31) == 0 && lines) atomicAdd(&sm.lines, 4 * lines);
+    // notifications, as in the scalar pass
+    const bool fresh = dirty_in & D_FRESH;
+    if (anych || fresh) {
+        const int c8 = conn8 ? 1 : 0;
+        for (int x = threadIdx.x; x < TW; x += NW * 32) {
+            uint8_t v = O(0, x);
+            if (fresh || v != sm.eN[x])
+                for (int d = -c8; d <= c8; ++d) {
+                    const int h = x + d;
+                    if (h < 0 || h >= TW) continue;
+                    const uint8_t hv = O(-1, h);
+                    if (v > hv && sm.mN[h + 1] > hv) my_edges |= 1u;
+                }
+            v = O(TH - 1, x);
+            if (fresh || v != sm.eS[x])
+                for (int d = -c8; d <= c8; ++d) {
+                    const int h = x + d;
+                    if (h < 0 || h >= TW) continue;
+                    const uint8_t hv = O(TH, h);
+                    if (v > hv && sm.mS[h + 1] > hv) my_edges |= 2u;
+                }
+        }
+        for (int y = threadIdx.x; y < TH; y += NW * 32) {
+            uint8_t v = O(y, 0);
+            if (fresh || v != sm.eW[y])
+                for (int d = -c8; d <= c8; ++d) {
+                    const int h = y + d;
+                    if (h < 0 || h >= TH) continue;
+                    const uint8_t hv = O(h, -1);
+                    if (v > hv && sm.mW[h] > hv) my_edges |= 4u;
+                }
+            v = O(y, TW - 1);
+            if (fresh || v != sm.eE[y])
+                for (int d = -c8; d <= c8; ++d) {
+                    const int h = y + d;
+                    if (h < 0 || h >= TH) continue;
+                    const uint8_t hv = O(h, TW);
+                    if (v > hv && sm.mE[h] > hv) my_edges |= 8u;
+                }
+        }
+        if (c8 && threadIdx.x == 0) {
+            uint8_t v, hv;
+            v = O(0, 0), hv = O(-1, -1);
+            if ((fresh || v != sm.eN[0]) && v > hv && sm.mN[0] > hv) my_edges |= 32u;
+            v = O(0, TW - 1), hv = O(-1, TW);
+            if ((fresh || v != sm.eN[TW - 1]) && v > hv && sm.mN[TW + 1] > hv) my_edges |= 64u;
+            v = O(TH - 1, 0), hv = O(TH, -1);
+            if ((fresh || v != sm.eS[0]) && v > hv && sm.mS[0] > hv) my_edges |= 128u;
+            v = O(TH - 1, TW - 1), hv = O(TH, TW);
+            if ((fresh || v != sm.eS[TW - 1]) && v > hv && sm.mS[TW + 1] > hv) my_edges |= 256u;
+        }
+    }
+    if (my_edges) atomicOr(&sm.edges, (int)my_edges);
+    if (anych)
+        for (int i = threadIdx.x; i < TH * TW; i += NW * 32) {
+            const int r = i / TW, cc = i - r * TW;
+            const int y = y0 + r, x = x0 + cc;
+            if (y < rows && x < cols) out[(int64_t)y * cols + x] = O(r, cc);
+        }
+    __threadfence();
+    __syncthreads();
+}
+
 // lane 0 only: mark the neighbour's dirty edge, then queue it
 __device__ __forceinline__ void notify(Queue &q, int t, int bits) {
     atomicOr(q.dirty + t, bits);
     q_push(q, t);
 }
 
-template <typename T, int TW, int TH, int P, int NW>
+template <typename T, int TW, int TH, int P, int NW, bool PACKED>
+using TileOf = typename std::conditional<PACKED, TileU8<TW, TH>, TileSmem<T, TW, TH, P>>::type;
+
+template <typename T, int TW, int TH, int P, int NW, bool PACKED>
 __global__ void __launch_bounds__(NW * 32, NW >= 16 ? 1 : 2) recon_cta(const T *__restrict__ mask, T *out, int rows, int cols, int conn,
                                                  int tiles_x, int tiles_y, Queue q) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
-    TileSmem<T, TW, TH, P> &sm = *reinterpret_cast<TileSmem<T, TW, TH, P> *>(sm_raw);
+    using Sm = TileOf<T, TW, TH, P, NW, PACKED>;
+    Sm &sm = *reinterpret_cast<Sm *>(sm_raw);
     const bool conn8 = conn == 8;
     for (;;) {
         if (threadIdx.x == 0) sm.tile = q_pop(q);
@@ -695,7 +1002,10 @@ __global__ void __launch_bounds__(NW * 32, NW >= 16 ? 1 : 2) recon_cta(const T *
             __syncthreads();
             const int dirty = sm.dirty;
             const int tx = t % tiles_x, ty = t / tiles_x;
-            cta_process_tile<T, TW, TH, P, NW>(mask, out, rows, cols, conn8, tx, ty, dirty, sm);
+            if constexpr (PACKED)
+                cta_process_tile_u8<TW, TH, NW>(mask, out, rows, cols, conn8, tx, ty, dirty, sm);
+            else
+                cta_process_tile<T, TW, TH, P, NW>(mask, out, rows, cols, conn8, tx, ty, dirty, sm);
             if (threadIdx.x == 0) {
                 const unsigned edges = (unsigned)sm.edges;
                 // our top edge is the upper tile's bottom halo, and so on
@@ -722,7 +1032,7 @@ __global__ void __launch_bounds__(NW * 32, NW >= 16 ? 1 : 2) recon_cta(const T *
     }
 }
 
-template <typename T, int TW, int TH, int P, int NW>
+template <typename T, int TW, int TH, int P, int NW, bool PACKED = false>
 int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int cols, int conn, cudaStream_t s) {
     NSG_TRY(check_dims(c, rows, cols));
     NSG_TRY(check_conn(c, conn));
@@ -783,8 +1093,8 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
     q.idle_limit = 2048;
     if (const char *e = getenv("NSG_RECON_IDLE")) q.idle_limit = atoi(e);  // tuning knob
     q.stats = c.ws.ctrl + C_RSTATS;
-    const size_t smem = sizeof(TileSmem<T, TW, TH, P>);
-    auto kfn = recon_cta<T, TW, TH, P, NW>;
+    const size_t smem = sizeof(TileOf<T, TW, TH, P, NW, PACKED>);
+    auto kfn = recon_cta<T, TW, TH, P, NW, PACKED>;
     NSG_CUDA_TRY(c, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     NSG_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, NW * 32, smem));
@@ -820,6 +1130,12 @@ int recon_warps() {
 int recon_u8(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t *out, int rows, int cols, int conn,
              cudaStream_t s) {
     const int nw = recon_warps();
+    bool packed = false;  // 4 x uint8 SIMD strips (tuning knob NSG_RECON_PACKED)
+    if (const char *e = getenv("NSG_RECON_PACKED")) packed = atoi(e) != 0;
+    if (packed) {
+        if (nw == 16) return run_recon_cta<uint8_t, 128, 128, 132, 16, true>(c, marker, mask, out, rows, cols, conn, s);
+        return run_recon_cta<uint8_t, 128, 128, 132, 8, true>(c, marker, mask, out, rows, cols, conn, s);
+    }
     if (nw == 8) return run_recon_cta<uint8_t, 128, 128, 132, 8>(c, marker, mask, out, rows, cols, conn, s);
     if (nw == 32) return run_recon_cta<uint8_t, 128, 128, 132, 32>(c, marker, mask, out, rows, cols, conn, s);
     return run_recon_cta<uint8_t, 128, 128, 132, 16>(c, marker, mask, out, rows, cols, conn, s);
