@@ -73,6 +73,20 @@ def dist_setup(args):
     return rank, world, local
 
 
+def replica_rate(px_per_rank, ms_local, world, device=None):
+    """Whole-job Mpixel/s of `world` replicas that each processed px_per_rank
+    pixels: the job takes as long as its slowest rank (max over ranks; no
+    other exchange).  Returns (Mpixel/s, ms of the slowest rank)."""
+    ms = ms_local
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms_local], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return world * px_per_rank / (ms / 1e3) / 1e6, ms
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -258,13 +272,7 @@ def run_nsg(args, rank, world, local):
     statuses = {}
     for i in range(len(tiles)):
         statuses[arr[i].status] = statuses.get(arr[i].status, 0) + 1
-    ms_step = total_ms / args.steps
-    if world > 1:
-        import torch.distributed as dist
-        tmax = torch.tensor([ms_step], dtype=torch.float64)
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        ms_step = float(tmax.item())
-    value = world * px / (ms_step / 1e3) / 1e6
+    value, ms_step = replica_rate(px, total_ms / args.steps, world, dev)
 
     # ---- e2e: host (pinned) tiles in, labels back to pinned host memory,
     # through the same batched entry point; copies inside the timed region
@@ -278,7 +286,7 @@ def run_nsg(args, rank, world, local):
     e2e_px = sum(t.shape[0] * t.shape[1] for t in e2e_tiles)
     pool.run(harr, params, host=True)
     e2e_ms = event_time(lambda: [pool.run(harr, params, host=True) for _ in range(args.steps)]) / args.steps
-    e2e_value = world * e2e_px / (e2e_ms / 1e3) / 1e6
+    e2e_value, _ = replica_rate(e2e_px, e2e_ms, world, dev)
     pool.close()
 
     # ---- per-tile form: the same tiles one call at a time on one stream,
