@@ -155,20 +155,27 @@ __global__ void k_classify(PW a) {
         a.rlocal[p] = -1;
         a.rparent[p] = -2;
         a.isroot[p] = 0;
-        // per-domain arrays (indexed by domain id < n)
-        a.dsize[p] = 0;
-        a.bbx0[p] = INT_MAX;
-        a.bby0[p] = INT_MAX;
-        a.bbx1[p] = -1;
-        a.bby1[p] = -1;
-        a.dfirst[p] = ~0ull;
-        a.sup[p] = p;
-        a.mcount[p] = 0;
-        a.mfill[p] = 0;
-        a.icount[p] = 0;
-        a.ifill[p] = 0;
-        a.npop[p] = 0;
-        a.cut[p] = 0;
+    }
+}
+
+// per-domain arrays, once the number of domains is known (only those entries
+// are ever read: every consumer indexes them by a domain or group id)
+__global__ void k_domain_init(PW a, const int *nd_total) {
+    const int nd = *nd_total;
+    for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < nd; d += gridDim.x * blockDim.x) {
+        a.dsize[d] = 0;
+        a.bbx0[d] = INT_MAX;
+        a.bby0[d] = INT_MAX;
+        a.bbx1[d] = -1;
+        a.bby1[d] = -1;
+        a.dfirst[d] = ~0ull;
+        a.sup[d] = d;
+        a.mcount[d] = 0;
+        a.mfill[d] = 0;
+        a.icount[d] = 0;
+        a.ifill[d] = 0;
+        a.npop[d] = 0;
+        a.cut[d] = 0;
     }
 }
 
@@ -1362,6 +1369,8 @@ int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int 
     k_roots<<<g, kB, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
     NSG_TRY(exclusive_scan_i32(c, a.isroot, a.rank, n, a.ctl + W_ND, s));
+    k_domain_init<<<g, kB, 0, s>>>(a, a.ctl + W_ND);
+    NSG_COUNT_LAUNCH();
     k_domains<<<g, kB, 0, s>>>(a, a.ctl + W_ND);
     NSG_COUNT_LAUNCH();
     NSG_TRY(exclusive_scan_i32(c, a.dsize, a.doff, n, nullptr, s));
