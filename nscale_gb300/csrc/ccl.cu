@@ -110,6 +110,22 @@ __global__ void ccl_flatten(int *parent, int64_t n) {
         parent[i] = x;
     }
 }
+// the same, also clearing the per-component flag at every root (the first
+// step of the seed / border selections), and writing only changed links
+__global__ void ccl_flatten_zero(int *parent, int64_t n, int *__restrict__ flag) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int x0 = __ldcg(parent + i);
+        if (x0 < 0) continue;
+        int x = x0;
+        for (;;) {
+            int p = __ldcg(parent + x);
+            if (p == x) break;
+            x = p;
+        }
+        if (x != x0) parent[i] = x;
+        if (x == (int)i) flag[i] = 0;
+    }
+}
 
 // ---- block-local union-find ------------------------------------------------
 // A 32x32 tile is labelled in shared memory (union by atomicMin on local
@@ -414,8 +430,10 @@ __device__ int block_exclusive_scan(int v, int *sh, int *total) {
 }
 
 __global__ void __launch_bounds__(kScanThreads) scan_tiles(const int *__restrict__ in, int *__restrict__ out,
-                                                           int64_t n, int *__restrict__ block_sums) {
+                                                           int64_t n, int *__restrict__ block_sums,
+                                                           const int *__restrict__ d_len) {
     __shared__ int sh[33];
+    if (d_len && *d_len < n) n = *d_len;
     int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
     int v[kScanItems];
     int s = 0;
@@ -446,7 +464,8 @@ __global__ void __launch_bounds__(kScanThreads) scan_sums(int *sums, int nb, int
     }
     if (threadIdx.x == 0 && total) *total = carry;
 }
-__global__ void scan_add(int *out, int64_t n, const int *__restrict__ sums) {
+__global__ void scan_add(int *out, int64_t n, const int *__restrict__ sums, const int *__restrict__ d_len) {
+    if (d_len && *d_len < n) n = *d_len;
     int64_t base = (int64_t)blockIdx.x * kScanTile;
     int add = sums[blockIdx.x];
     for (int k = threadIdx.x; k < kScanTile; k += blockDim.x)
@@ -461,20 +480,24 @@ int blocks(Ctx &c, int64_t n) {
 
 }  // namespace
 
-int exclusive_scan_i32(Ctx &c, const int32_t *in, int32_t *out, int64_t n, int32_t *d_total, cudaStream_t s) {
+// d_len (nullable, device): scan only the first *d_len entries (at most n)
+int exclusive_scan_i32(Ctx &c, const int32_t *in, int32_t *out, int64_t n, int32_t *d_total, cudaStream_t s,
+                       const int32_t *d_len) {
     int nb = (int)((n + kScanTile - 1) / kScanTile);
     if (nb < 1) nb = 1;
-    scan_tiles<<<nb, kScanThreads, 0, s>>>(in, out, n, c.ws.scan_tmp);
+    scan_tiles<<<nb, kScanThreads, 0, s>>>(in, out, n, c.ws.scan_tmp, d_len);
     NSG_COUNT_LAUNCH();
     scan_sums<<<1, kScanThreads, 0, s>>>(c.ws.scan_tmp, nb, d_total);
     NSG_COUNT_LAUNCH();
-    scan_add<<<nb, 256, 0, s>>>(out, n, c.ws.scan_tmp);
+    scan_add<<<nb, 256, 0, s>>>(out, n, c.ws.scan_tmp, d_len);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
 
-int ccl_u8(Ctx &c, const uint8_t *img, int32_t *parent, int rows, int cols, int conn, int mode, cudaStream_t s) {
+// zero_flags (nullable): also clear flag[root] for every component root
+int ccl_u8(Ctx &c, const uint8_t *img, int32_t *parent, int rows, int cols, int conn, int mode, cudaStream_t s,
+           int *zero_flags) {
     int64_t n = (int64_t)rows * cols;
     PredU8 pr{img, mode};
     dim3 grid((cols + LT - 1) / LT, (rows + LT - 1) / LT);
@@ -482,7 +505,10 @@ int ccl_u8(Ctx &c, const uint8_t *img, int32_t *parent, int rows, int cols, int 
     NSG_COUNT_LAUNCH();
     ccl_border<PredU8><<<blocks(c, n), kB, 0, s>>>(pr, parent, rows, cols, conn);
     NSG_COUNT_LAUNCH();
-    ccl_flatten<<<blocks(c, n), kB, 0, s>>>(parent, n);
+    if (zero_flags)
+        ccl_flatten_zero<<<blocks(c, n), kB, 0, s>>>(parent, n, zero_flags);
+    else
+        ccl_flatten<<<blocks(c, n), kB, 0, s>>>(parent, n);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
@@ -525,10 +551,8 @@ int recon_binary_dev(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t
                      cudaStream_t s) {
     int64_t n = (int64_t)rows * cols;
     int *lab = c.ws.i32[0], *flag = c.ws.i32[1];
-    NSG_TRY(ccl_u8(c, mask, lab, rows, cols, conn, CCL_NONZERO, s));
+    NSG_TRY(ccl_u8(c, mask, lab, rows, cols, conn, CCL_NONZERO, s, flag));
     int g = blocks(c, n);
-    zero_flags_at_roots<<<g, kB, 0, s>>>(lab, flag, n);
-    NSG_COUNT_LAUNCH();
     flag_seeds<<<g, kB, 0, s>>>(lab, marker, mask, flag, n);
     NSG_COUNT_LAUNCH();
     select_recon<<<g, kB, 0, s>>>(lab, flag, marker, mask, out, n);
@@ -541,10 +565,8 @@ int bwselect_dev(Ctx &c, const uint8_t *bw, const uint8_t *seeds, uint8_t *out, 
                  cudaStream_t s) {
     int64_t n = (int64_t)rows * cols;
     int *lab = c.ws.i32[0], *flag = c.ws.i32[1];
-    NSG_TRY(ccl_u8(c, bw, lab, rows, cols, conn, CCL_NONZERO, s));
+    NSG_TRY(ccl_u8(c, bw, lab, rows, cols, conn, CCL_NONZERO, s, flag));
     int g = blocks(c, n);
-    zero_flags_at_roots<<<g, kB, 0, s>>>(lab, flag, n);
-    NSG_COUNT_LAUNCH();
     flag_seeds<<<g, kB, 0, s>>>(lab, seeds, bw, flag, n);
     NSG_COUNT_LAUNCH();
     select_bw<<<g, kB, 0, s>>>(lab, flag, bw, out, n);
@@ -556,10 +578,8 @@ int bwselect_dev(Ctx &c, const uint8_t *bw, const uint8_t *seeds, uint8_t *out, 
 int fill_holes_dev(Ctx &c, const uint8_t *img, uint8_t *out, int rows, int cols, int conn, cudaStream_t s) {
     int64_t n = (int64_t)rows * cols;
     int *lab = c.ws.i32[0], *flag = c.ws.i32[1];
-    NSG_TRY(ccl_u8(c, img, lab, rows, cols, conn, CCL_NOT255, s));
+    NSG_TRY(ccl_u8(c, img, lab, rows, cols, conn, CCL_NOT255, s, flag));
     int g = blocks(c, n);
-    zero_flags_at_roots<<<g, kB, 0, s>>>(lab, flag, n);
-    NSG_COUNT_LAUNCH();
     flag_border<<<blocks(c, 2 * (int64_t)rows + 2 * cols), kB, 0, s>>>(lab, flag, rows, cols);
     NSG_COUNT_LAUNCH();
     select_fill<<<g, kB, 0, s>>>(lab, flag, out, n);

@@ -198,7 +198,8 @@ int recon_f32(Ctx &c, const float *marker, const float *mask, float *out, int ro
               cudaStream_t s);
 // ccl.cu (uses i32[0..1] unless an output array doubles as the parent array)
 enum CclMode { CCL_EQUAL = 0, CCL_NONZERO = 1, CCL_NOT255 = 2 };
-int ccl_u8(Ctx &c, const uint8_t *img, int32_t *parent, int rows, int cols, int conn, int mode, cudaStream_t s);
+int ccl_u8(Ctx &c, const uint8_t *img, int32_t *parent, int rows, int cols, int conn, int mode, cudaStream_t s,
+           int *zero_flags = nullptr);
 int ccl_f32_masked(Ctx &c, const float *val, const uint8_t *valid, int32_t *parent, int rows, int cols, int conn,
                    cudaStream_t s);
 int bwareaopen_dev(Ctx &c, const uint8_t *img, uint8_t *out, int rows, int cols, int min_size, int max_size,
@@ -211,7 +212,8 @@ int fill_holes_dev(Ctx &c, const uint8_t *img, uint8_t *out, int rows, int cols,
 int bwlabel_dev(Ctx &c, const uint8_t *img, int32_t *labels, int rows, int cols, int conn, cudaStream_t s);
 int bbox_dev(Ctx &c, const int32_t *labels, int rows, int cols, int32_t *d_bbox, int64_t cap_ints, int *d_count,
              cudaStream_t s);
-int exclusive_scan_i32(Ctx &c, const int32_t *in, int32_t *out, int64_t n, int32_t *d_total, cudaStream_t s);
+int exclusive_scan_i32(Ctx &c, const int32_t *in, int32_t *out, int64_t n, int32_t *d_total, cudaStream_t s,
+                       const int32_t *d_len = nullptr);
 // edt.cu (uses i32[2])
 int dist_transform_dev(Ctx &c, const uint8_t *mask, float *dist, int rows, int cols, cudaStream_t s);
 // minima.cu (uses f32[0..2], i32[0..1], u8[0])

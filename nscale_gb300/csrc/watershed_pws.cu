@@ -1373,7 +1373,7 @@ int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int 
     NSG_COUNT_LAUNCH();
     k_domains<<<g, kB, 0, s>>>(a, a.ctl + W_ND);
     NSG_COUNT_LAUNCH();
-    NSG_TRY(exclusive_scan_i32(c, a.dsize, a.doff, n, nullptr, s));
+    NSG_TRY(exclusive_scan_i32(c, a.dsize, a.doff, n, nullptr, s, a.ctl + W_ND));  // per-domain: nd entries
     NSG_LAUNCH_CHECK(c);
     // P1: one thread per domain (the grid covers the largest possible count)
     const int gd = c.sm_count * 32;  // per-domain kernels: grid-stride over the domain count
@@ -1414,12 +1414,12 @@ int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int 
     NSG_COUNT_LAUNCH();
     k_groups<<<g, kB, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
-    NSG_TRY(exclusive_scan_i32(c, a.mcount, a.moff, n, nullptr, s));
+    NSG_TRY(exclusive_scan_i32(c, a.mcount, a.moff, n, nullptr, s, a.ctl + W_ND));
     k_groups2<<<g, kB, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
     k_inj_count<<<g, kB, 0, s>>>(a, 0);
     NSG_COUNT_LAUNCH();
-    NSG_TRY(exclusive_scan_i32(c, a.icount, a.ioff, n, nullptr, s));
+    NSG_TRY(exclusive_scan_i32(c, a.icount, a.ioff, n, nullptr, s, a.ctl + W_ND));
     k_inj_count<<<g, kB, 0, s>>>(a, 1);
     NSG_COUNT_LAUNCH();
     k_reset_owned_u<<<g, kB, 0, s>>>(a);
