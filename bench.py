@@ -43,6 +43,10 @@ METRIC = "segmentNuclei Mpixel/s on 1 GB300, batched vs per-tile; p50/p99 tile l
 # minima 17, bwlabel 5, watershed 12, border+mask 6, area-open 14, fill 2,
 # bwlabel 5)
 ALG_BYTES_PER_PX = 137
+# measured DRAM reads + writes per pixel of the same pipeline: ncu
+# dram__bytes_read.sum + dram__bytes_write.sum summed over every kernel of
+# one 2048 x 2048 tile run to SUCCESS (python -m nscale_gb300.tile_demo 2048)
+DRAM_BYTES_PER_PX = 401.1
 
 
 
@@ -375,7 +379,10 @@ def run_nsg(args, rank, world, local):
         "roofline": {"bound": "hbm", "kernel": "segmentNuclei pipeline, all stages (batched)",
                      "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 5), "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_px": ALG_BYTES_PER_PX, "traffic": None},
+                     "algorithmic_bytes_per_px": ALG_BYTES_PER_PX,
+                     "traffic": int(DRAM_BYTES_PER_PX * px),
+                     "traffic_note": f"DRAM bytes per step: {DRAM_BYTES_PER_PX} B/px measured by ncu over all "
+                                     f"kernels of one 2048x2048 tile, x pixels per step"},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mpixel/s", "h2d_bytes_per_step": int(3 * e2e_px),
                 "d2h_bytes_per_step": int(4 * e2e_px), "tiles": len(e2e_tiles)},
         "gpu_launches": int(launches),
