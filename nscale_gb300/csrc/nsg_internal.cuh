@@ -91,6 +91,7 @@ struct Ctx {
     int sm_count = 0;
     long long spin_budget = 1ll << 26;
     cudaEvent_t ev_counts = nullptr;  // marks a posted readback of the device counters
+    int recon_max_ctas = 0;           // cap on the reconstruction's persistent grid (0: one CTA per SM)
     std::string last_error;
 };
 

@@ -984,7 +984,7 @@ template <typename T, int TW, int TH, int P, int NW, bool PACKED>
 using TileOf = typename std::conditional<PACKED, TileU8<TW, TH>, TileSmem<T, TW, TH, P>>::type;
 
 template <typename T, int TW, int TH, int P, int NW, bool PACKED>
-__global__ void __launch_bounds__(NW * 32, NW >= 16 ? 1 : 2) recon_cta(const T *__restrict__ mask, T *out, int rows, int cols, int conn,
+__global__ void __launch_bounds__(NW * 32, (NW >= 16 && !PACKED) ? 1 : 2) recon_cta(const T *__restrict__ mask, T *out, int rows, int cols, int conn,
                                                  int tiles_x, int tiles_y, Queue q) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     using Sm = TileOf<T, TW, TH, P, NW, PACKED>;
@@ -1105,6 +1105,10 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
     if (want >= 1 && want < per_sm) per_sm = want;
     if (per_sm < 1) per_sm = 1;
     int grid = c.sm_count * per_sm;
+    // a context that shares the GPU with other tiles in flight (a pool worker)
+    // runs its reconstructions on part of the SMs: the queue's CTA-time is
+    // about the same on fewer CTAs, and the other tiles get the rest
+    if (c.recon_max_ctas > 0 && c.recon_max_ctas < grid) grid = c.recon_max_ctas;
     if (const char *e = getenv("NSG_RECON_MAX_CTAS")) {  // tuning knob: cap on the persistent grid
         const int v = atoi(e);
         if (v >= 1 && v < grid) grid = v;
