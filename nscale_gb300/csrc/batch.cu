@@ -7,9 +7,9 @@
 // per-domain floods, the tail of the reconstruction queue), so the pool keeps
 // several tiles in flight and lets their stages overlap:
 //
-//  * nsg_segment_nuclei_batch: every worker takes the next tile index from a
-//    shared counter until the batch is done (largest-first order is the
-//    caller's choice);
+//  * nsg_segment_nuclei_batch: every worker takes the next tile from a shared
+//    counter over the tiles sorted largest first, so that the batch ends on
+//    small tiles;
 //  * nsg_server_*: tiles are submitted one at a time into a bounded FIFO and
 //    results are polled; the number of workers is what a memory budget admits.
 //
@@ -129,6 +129,7 @@ struct nsg_pool {
     // batch job (published under mu, then read lock-free by the workers)
     nsg_tile *tiles = nullptr;
     int n = 0;
+    std::vector<int> order;  // tiles largest first: the batch's tail is a small tile
     nsg_seg_params prm{};
     int flags = 0;
     std::atomic<int> next{0};
@@ -170,8 +171,9 @@ struct nsg_pool {
             lk.unlock();
             const bool host = flags & NSG_TILE_HOST;
             for (;;) {
-                const int i = next.fetch_add(1);
-                if (i >= n) break;
+                const int k = next.fetch_add(1);
+                if (k >= n) break;
+                const int i = order[k];
                 run_tile(me.ctx, me.stream, tiles[i], prm, host);
                 if (tiles[i].status < NSG_RUNTIME_FAILED) {
                     int zero = 0;
@@ -258,6 +260,11 @@ int nsg_segment_nuclei_batch(nsg_pool *p, nsg_tile *tiles, int n, const nsg_seg_
     if (p->busy) return NSG_ERR_ARG;  // one batch at a time per pool
     p->tiles = tiles;
     p->n = n;
+    p->order.resize(n);
+    for (int i = 0; i < n; ++i) p->order[i] = i;
+    std::stable_sort(p->order.begin(), p->order.end(), [&](int a, int b) {
+        return (int64_t)tiles[a].rows * tiles[a].cols > (int64_t)tiles[b].rows * tiles[b].cols;
+    });
     if (prm) p->prm = *prm;
     else nsg_default_params(&p->prm);
     p->flags = flags;
