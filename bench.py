@@ -61,7 +61,8 @@ def parse():
                     help="tiles in flight: pool workers, each with its own context and CUDA stream")
     ap.add_argument("--per-tile-tiles", type=int, default=64, help="tiles timed in the per-tile comparison")
     ap.add_argument("--serve-tiles", type=int, default=96, help="tiles sent through the server (0 = skip)")
-    ap.add_argument("--serve-load", type=float, default=0.7, help="offered load, fraction of batched throughput")
+    ap.add_argument("--serve-load", default="0.3,0.7,0.95",
+                    help="offered loads to sweep, fractions of the batched throughput (comma list)")
     ap.add_argument("--cpu-sample-tiles", type=int, default=0, help="tiles in the CPU baseline sample (0 = cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -420,33 +421,38 @@ def serve(args, tiles, batched_mpx_s):
     per = _lib.load().nsg_pool_context_bytes(maxr, maxc)
     srv = TileServer(maxr, maxc, memory_budget_bytes=per * max(1, args.streams), queue_cap=len(host))
     mean_px = sum(h.shape[0] * h.shape[1] for h in host) / len(host)
-    rate = args.serve_load * batched_mpx_s * 1e6 / mean_px  # tiles per second
-    rng = random.Random(0x5EED0004)
-    results = []
-    t0 = time.perf_counter()
-    due = t0
-    for h, lab in zip(host, labs):
-        due += rng.expovariate(rate)
-        while time.perf_counter() < due:
-            results += srv.poll(64, 0)
-            time.sleep(min(0.0005, max(0.0, due - time.perf_counter())))
-        srv.submit(h, lab, want_features=True)
-    while len(results) < len(host):
-        results += srv.poll(64, 100)
-    wall = time.perf_counter() - t0
+    runs = []
+    for load in [float(x) for x in str(args.serve_load).split(",") if x]:
+        rate = load * batched_mpx_s * 1e6 / mean_px  # tiles per second
+        rng = random.Random(0x5EED0004)
+        results = []
+        t0 = time.perf_counter()
+        due = t0
+        for h, lab in zip(host, labs):
+            due += rng.expovariate(rate)
+            while time.perf_counter() < due:
+                results += srv.poll(64, 0)
+                time.sleep(min(0.0005, max(0.0, due - time.perf_counter())))
+            srv.submit(h, lab, want_features=True)
+        while len(results) < len(host):
+            results += srv.poll(64, 100)
+        wall = time.perf_counter() - t0
+        lat = sorted(r["latency_ms"] for r in results)
+        st = {}
+        for r in results:
+            st[str(r["status"])] = st.get(str(r["status"]), 0) + 1
+        nfeat = sum(len(r["features"]) for r in results if r["features"] is not None)
+        runs.append({"load": load, "offered_tiles_per_s": round(rate, 2),
+                     "achieved_tiles_per_s": round(len(host) / wall, 2),
+                     "achieved_mpx_s": round(sum(h.shape[0] * h.shape[1] for h in host) / wall / 1e6, 2),
+                     "p50_ms": round(lat[len(lat) // 2], 3),
+                     "p99_ms": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3),
+                     "statuses": st, "nuclei_with_features": nfeat})
     workers = srv.workers
     srv.close()
-    lat = sorted(r["latency_ms"] for r in results)
-    st = {}
-    for r in results:
-        st[str(r["status"])] = st.get(str(r["status"]), 0) + 1
-    nfeat = sum(len(r["features"]) for r in results if r["features"] is not None)
-    return {"tiles": len(host), "arrivals": "poisson", "offered_tiles_per_s": round(rate, 2),
-            "statuses": st, "nuclei_with_features": nfeat,
-            "output": "labels + per-nucleus area, perimeter, mean/std H, mean gradient",
-            "load": args.serve_load, "workers": workers,
-            "p50_ms": round(lat[len(lat) // 2], 3), "p99_ms": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3),
-            "achieved_tiles_per_s": round(len(host) / wall, 2)}
+    return {"tiles_per_run": len(host), "arrivals": "poisson", "workers": workers,
+            "output": "labels + per-nucleus area, perimeter, mean/std H, mean gradient; every 5th tile tissue-free",
+            "runs": runs}
 
 
 def main():
