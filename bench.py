@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--streams", type=int, default=8,
                     help="tiles in flight: pool workers, each with its own context and CUDA stream")
     ap.add_argument("--per-tile-tiles", type=int, default=64, help="tiles timed in the per-tile comparison")
+    ap.add_argument("--autotune-tiles", type=int, default=32,
+                    help="tiles of the batch the autotuner measures launch shapes on (0 = defaults)")
     ap.add_argument("--serve-tiles", type=int, default=96, help="tiles sent through the server (0 = skip)")
     ap.add_argument("--serve-load", default="0.3,0.7,0.95",
                     help="offered loads to sweep, fractions of the batched throughput (comma list)")
@@ -260,7 +262,15 @@ def run_nsg(args, rank, world, local):
         return ev0.elapsed_time(ev1)
 
     # ---- batched form: every tile of the batch on the pool's workers --------
+    tuning = None
+    if args.autotune_tiles > 0:
+        # launch shapes picked on the first tiles of the batch (results do not depend on them)
+        from nscale_gb300.autotune import autotune
+        tuning = autotune(tiles[: args.autotune_tiles], device=local)
+        args.streams = tuning["workers"]
     pool = TilePool(maxr, maxc, workers=max(1, args.streams), device=local)
+    if tuning:
+        pool.set_tuning(tuning["recon_max_ctas"], tuning["bfs_max_cluster"])
     labels = [torch.empty(t.shape[0] * t.shape[1], dtype=torch.int32, device=dev) for t in tiles]
     arr = (_lib.Tile * len(tiles))()
     for i, t in enumerate(tiles):
@@ -368,6 +378,9 @@ def run_nsg(args, rank, world, local):
                    "tiles": len(tiles), "pixels_per_step": px,
                    "form": f"batched: nsg_segment_nuclei_batch, {pool_workers(args)} tiles in flight "
                            f"(one context and stream per worker)",
+                   "tuning": ({k: tuning[k] for k in ("workers", "recon_max_ctas", "bfs_max_cluster")}
+                              | {"picked_from": len(tuning["trials"]), "calibration_tiles": tuning["calibration_tiles"]}
+                              if tuning else "defaults"),
                    "l2": "inputs larger than L2 (5.6 GB per step)", "parallelism": f"replicas x{world}"},
         "per_tile": {"value": round(pt_value, 3), "unit": "Mpixel/s", "tiles": n_pt,
                      "form": "nsg_segment_nuclei one tile at a time on one stream",

@@ -76,6 +76,16 @@ size_t nsg_context_bytes(const nsg_context *ctx);
 /* Device-wait budget for persistent kernels (iterations); tests set it low to
  * exercise NSG_ERR_TIMEOUT.  0 restores the default. */
 int nsg_context_set_spin_budget(nsg_context *ctx, long long iterations);
+/* Launch-shape tuning (no counterpart in the reference, whose kernels have
+ * fixed shapes): results do not depend on it.  recon_max_ctas caps the
+ * grey reconstruction's persistent grid (0 = one CTA per SM);
+ * bfs_max_cluster is the largest thread-block cluster the watershed BFS
+ * tries (1-16, 0 = 16).  nscale_gb300.autotune measures and picks them. */
+typedef struct nsg_tuning {
+    int recon_max_ctas;
+    int bfs_max_cluster;
+} nsg_tuning;
+int nsg_context_set_tuning(nsg_context *ctx, const nsg_tuning *t);
 
 /* ---- PixelOperations / HistologicalEntities helpers ---------------------- */
 /* HistologicalEntities::getBackground (HistologicalEntities.cpp:93-109):
@@ -262,6 +272,9 @@ typedef struct nsg_pool nsg_pool;
 int nsg_pool_create(nsg_pool **pool, int max_rows, int max_cols, int workers, int device);
 int nsg_pool_destroy(nsg_pool *pool);
 int nsg_pool_workers(const nsg_pool *pool);
+/* the same tuning on every worker's context (between batches); a pool's
+ * default caps each reconstruction at half the SMs */
+int nsg_pool_set_tuning(nsg_pool *pool, const nsg_tuning *t);
 /* segmentNuclei on every tile of `tiles` (any order, all workers); returns
  * when all are done.  Per-tile statuses land in tiles[i].status; the return
  * value is NSG_SUCCESS or the first NSG_ERR_* a tile produced.  p NULL =

@@ -43,6 +43,12 @@ class SegParams(C.Structure):
             setattr(self, k, v)
 
 
+class Tuning(C.Structure):
+    """nsg_tuning: launch shapes (results do not depend on them)."""
+
+    _fields_ = [("recon_max_ctas", C.c_int), ("bfs_max_cluster", C.c_int)]
+
+
 class Tile(C.Structure):
     """nsg_tile: one tile of a batch or server submission (include/nsg.h)."""
 
@@ -90,6 +96,8 @@ _SIGS = {
     "nsg_pool_create": (_I, [C.POINTER(_P), _I, _I, _I, _I]),
     "nsg_pool_destroy": (_I, [_P]),
     "nsg_pool_workers": (_I, [_P]),
+    "nsg_pool_set_tuning": (_I, [_P, C.POINTER(Tuning)]),
+    "nsg_context_set_tuning": (_I, [_P, C.POINTER(Tuning)]),
     "nsg_pool_context_bytes": (C.c_size_t, [_I, _I]),
     "nsg_segment_nuclei_batch": (_I, [_P, C.POINTER(Tile), _I, C.POINTER(SegParams), _I]),
     "nsg_server_create": (_I, [C.POINTER(_P), _I, _I, C.c_size_t, _I, _I]),

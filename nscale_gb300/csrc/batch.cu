@@ -253,6 +253,17 @@ int nsg_pool_destroy(nsg_pool *p) {
 
 int nsg_pool_workers(const nsg_pool *p) { return p ? (int)p->w.size() : 0; }
 
+int nsg_pool_set_tuning(nsg_pool *p, const nsg_tuning *t) {
+    if (!p || !t) return NSG_ERR_ARG;
+    std::lock_guard<std::mutex> lk(p->mu);
+    if (p->busy) return NSG_ERR_ARG;  // not while a batch runs
+    for (auto &w : p->w) {
+        const int r = nsg_context_set_tuning(w.ctx, t);
+        if (r != NSG_SUCCESS) return r;
+    }
+    return NSG_SUCCESS;
+}
+
 int nsg_segment_nuclei_batch(nsg_pool *p, nsg_tile *tiles, int n, const nsg_seg_params *prm, int flags) {
     if (!p || n < 0 || (n > 0 && !tiles)) return NSG_ERR_ARG;
     if (n == 0) return NSG_SUCCESS;

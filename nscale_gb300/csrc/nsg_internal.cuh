@@ -92,6 +92,7 @@ struct Ctx {
     long long spin_budget = 1ll << 26;
     cudaEvent_t ev_counts = nullptr;  // marks a posted readback of the device counters
     int recon_max_ctas = 0;           // cap on the reconstruction's persistent grid (0: one CTA per SM)
+    int bfs_max_cluster = 0;          // largest BFS thread-block cluster tried (0: 16)
     std::string last_error;
 };
 

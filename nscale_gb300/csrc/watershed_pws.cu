@@ -1320,6 +1320,7 @@ static int launch_bfs(Ctx &c, const PW &a, const uint8_t *nbm, cudaStream_t s) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int cl = kBfsMaxCluster;
+    if (c.bfs_max_cluster >= 1 && c.bfs_max_cluster < cl) cl = c.bfs_max_cluster;
     if (const char *e = getenv("NSG_BFS_CLUSTER")) {  // tuning knob: largest cluster to try
         const int v = atoi(e);
         if (v >= 1 && v <= kBfsMaxCluster) cl = v;

@@ -52,6 +52,11 @@ class TilePool:
     def workers(self) -> int:
         return self.L.nsg_pool_workers(self.h)
 
+    def set_tuning(self, recon_max_ctas: int = 0, bfs_max_cluster: int = 0) -> None:
+        """nsg_pool_set_tuning: launch shapes of every worker (results do not change)."""
+        t = _lib.Tuning(recon_max_ctas, bfs_max_cluster)
+        _check(self.L.nsg_pool_set_tuning(self.h, C.byref(t)), "nsg_pool_set_tuning")
+
     def run(self, tiles: "C.Array", params: _lib.SegParams | None = None, host: bool = False) -> int:
         """nsg_segment_nuclei_batch over a prepared ctypes array of Tile."""
         rc = self.L.nsg_segment_nuclei_batch(self.h, tiles, len(tiles), C.byref(params) if params else None,

@@ -137,3 +137,20 @@ def test_server_features_match_feature_entry(cuda):
     finally:
         pool.close()
     assert st == 0 and np.array_equal(lab2.cpu().numpy(), lab) and np.array_equal(feats, want)
+
+
+def test_tuning_changes_no_result(cuda):
+    """Launch shapes (reconstruction grid, BFS cluster) change speed only."""
+    import torch
+    from nscale_gb300.serving import TilePool
+    tiles = [torch.from_numpy(t).cuda() for t in _tiles()[:3]]
+    pool = TilePool(1024, 1500, workers=2)
+    try:
+        base = pool.segment(tiles)
+        pool.set_tuning(recon_max_ctas=7, bfs_max_cluster=2)
+        tuned = pool.segment(tiles)
+    finally:
+        pool.close()
+    for (s0, l0, n0, b0), (s1, l1, n1, b1) in zip(base, tuned):
+        assert s0 == s1 and n0 == n1
+        assert torch.equal(l0, l1) and np.array_equal(b0, b1)
