@@ -34,6 +34,9 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# 32 hardware work queues for the tiles in flight (read when the CUDA context
+# is created; nscale_gb300 sets the same default on import)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = "segmentNuclei Mpixel/s on 1 GB300, batched vs per-tile; p50/p99 tile latency"
 # algorithmic bytes per pixel of a tile that runs to SUCCESS: each spatial
@@ -57,10 +60,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="nsg", choices=["nsg", "reference"])
     ap.add_argument("--tiles", type=int, default=256)
-    ap.add_argument("--streams", type=int, default=8,
+    ap.add_argument("--streams", type=int, default=32,
                     help="tiles in flight: pool workers, each with its own context and CUDA stream")
     ap.add_argument("--per-tile-tiles", type=int, default=64, help="tiles timed in the per-tile comparison")
-    ap.add_argument("--autotune-tiles", type=int, default=32,
+    ap.add_argument("--autotune-tiles", type=int, default=96,
                     help="tiles of the batch the autotuner measures launch shapes on (0 = defaults)")
     ap.add_argument("--serve-tiles", type=int, default=96, help="tiles sent through the server (0 = skip)")
     ap.add_argument("--serve-load", default="0.3,0.7,0.95",
@@ -268,6 +271,9 @@ def run_nsg(args, rank, world, local):
         from nscale_gb300.autotune import autotune
         tuning = autotune(tiles[: args.autotune_tiles], device=local)
         args.streams = tuning["workers"]
+    else:
+        from nscale_gb300.autotune import max_workers
+        args.streams = min(args.streams, max_workers(maxr, maxc, local))
     pool = TilePool(maxr, maxc, workers=max(1, args.streams), device=local)
     if tuning:
         pool.set_tuning(tuning["recon_max_ctas"], tuning["bfs_max_cluster"])
@@ -276,8 +282,12 @@ def run_nsg(args, rank, world, local):
     for i, t in enumerate(tiles):
         arr[i].bgr, arr[i].rows, arr[i].cols, arr[i].row_stride_bytes = t.data_ptr(), t.shape[0], t.shape[1], 0
         arr[i].labels, arr[i].mask, arr[i].want_bbox = labels[i].data_ptr(), None, 0
-    for _ in range(args.warmup):
+    for w in range(args.warmup):
+        if w == args.warmup - 1:  # per-stage times under contention, from the last warm-up pass
+            pool.set_timing(True)
         pool.run(arr, params)
+    batched_stages, batched_timed = pool.stage_times()
+    pool.set_timing(False)
     barrier()
     launches0 = L.nsg_kernel_launches()
     with Clocks(local) as clk:
@@ -338,13 +348,13 @@ def run_nsg(args, rank, world, local):
         ev1.record(stream)
         torch.cuda.synchronize()
         pt_ms = ev0.elapsed_time(ev1)
-        stage_ms = (C.c_double * 19)()
+        stage_ms = (C.c_double * 32)()
         calls = C.c_longlong(0)
-        L.nsg_context_stage_times(ctx.h, stage_ms, 19, C.byref(calls))
+        n_stages = L.nsg_context_stage_times(ctx.h, stage_ms, 32, C.byref(calls))
         L.nsg_context_set_timing(ctx.h, 0)
         per_tile(record=True)  # latency of one tile alone
-    names = [L.nsg_stage_name(i).decode() for i in range(19)]
-    per_stage = {names[i]: stage_ms[i] for i in range(19)}
+    names = [L.nsg_stage_name(i).decode() for i in range(n_stages)]
+    per_stage = {names[i]: stage_ms[i] for i in range(n_stages)}
     pt_value = pt_px / (pt_ms / 1e3) / 1e6
     ctx.close()
 
@@ -390,6 +400,8 @@ def run_nsg(args, rank, world, local):
                        "what": "one tile alone, per-tile form"},
         "statuses": {str(k): v for k, v in statuses.items()},
         "stage_ms_per_tile_pass": {k: round(v, 3) for k, v in per_stage.items() if v > 0},
+        "stage_ms_per_tile_batched": {k: round(v / max(1, batched_timed), 3)
+                                      for k, v in batched_stages.items() if v > 0},
         "roofline": {"bound": "hbm", "kernel": "segmentNuclei pipeline, all stages (batched)",
                      "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 5), "peak_kind": peak_kind,
@@ -434,6 +446,13 @@ def serve(args, tiles, batched_mpx_s):
     per = _lib.load().nsg_pool_context_bytes(maxr, maxc)
     srv = TileServer(maxr, maxc, memory_budget_bytes=per * max(1, args.streams), queue_cap=len(host))
     mean_px = sum(h.shape[0] * h.shape[1] for h in host) / len(host)
+    # warm-up: every worker runs tiles once (first-use set-up stays out of the latencies)
+    warm = min(len(host), 2 * srv.workers)
+    for h, lab in zip(host[:warm], labs[:warm]):
+        srv.submit(h, lab, want_features=True)
+    got = 0
+    while got < warm:
+        got += len(srv.poll(64, 100))
     runs = []
     for load in [float(x) for x in str(args.serve_load).split(",") if x]:
         rate = load * batched_mpx_s * 1e6 / mean_px  # tiles per second

@@ -310,9 +310,16 @@ int nsg_server_destroy(nsg_server *srv);
  * SimpleCSVLogger::logTimeSinceLastLog (UtilsLogger.h:85-183; stage names as
  * HistologicalEntities.cpp logs them).  Enabling resets the accumulators;
  * nsg_context_stage_times copies up to n accumulated milliseconds and returns
- * the number of stages; nsg_stage_name gives stage i's name. */
+ * the number of stages; nsg_stage_name gives stage i's name.  Stages 19-21
+ * (watershed_P1, watershed_BFS, watershed_P3) split the watershed's flood;
+ * "watershed" keeps the rest of that stage. */
 int nsg_context_set_timing(nsg_context *ctx, int on);
 int nsg_context_stage_times(nsg_context *ctx, double *ms_out, int n, long long *calls);
+/* The same for every worker of a pool (summed over workers; calls = tiles
+ * timed).  In the batched form a stage's time includes the waits for SMs
+ * that the other tiles in flight hold.  Not while a batch runs. */
+int nsg_pool_set_timing(nsg_pool *pool, int on);
+int nsg_pool_stage_times(nsg_pool *pool, double *ms_out, int n, long long *calls);
 const char *nsg_stage_name(int i);
 
 /* Number of CUDA kernels this library has launched in this process. */

@@ -122,6 +122,8 @@ _SIGS = {
                                      C.POINTER(C.POINTER(C.c_int32)), _P]),
     "nsg_context_set_timing": (_I, [_P, _I]),
     "nsg_context_stage_times": (_I, [_P, C.POINTER(C.c_double), _I, C.POINTER(C.c_longlong)]),
+    "nsg_pool_set_timing": (_I, [_P, _I]),
+    "nsg_pool_stage_times": (_I, [_P, C.POINTER(C.c_double), _I, C.POINTER(C.c_longlong)]),
     "nsg_stage_name": (C.c_char_p, [_I]),
     "nsg_kernel_launches": (C.c_longlong, []),
     "nsg_alloc": (_P, [C.c_size_t]),

@@ -18,8 +18,8 @@ import torch
 from . import _lib
 from .serving import TilePool
 
-WORKERS = (6, 8, 12)
-RECON_FRACTIONS = (0.25, 0.5)
+WORKERS = (16, 24, 32)
+RECON_FRACTIONS = (1 / 16, 1 / 8, 1 / 4)
 BFS_CLUSTERS = (16,)
 
 
@@ -34,6 +34,15 @@ def _tile_array(tiles):
     return arr, labels
 
 
+def max_workers(max_rows: int, max_cols: int, device: int = 0, reserve: float = 0.25) -> int:
+    """Pool workers whose contexts fit in the device's free memory, keeping
+    `reserve` of it (and at least 8 GiB) for the tiles and the caller."""
+    free, _total = torch.cuda.mem_get_info(device)
+    per = _lib.load().nsg_pool_context_bytes(max_rows, max_cols)
+    usable = free - max(int(free * reserve), 8 << 30)
+    return max(1, int(usable // per)) if per > 0 else 1
+
+
 def autotune(tiles, workers=WORKERS, recon_fractions=RECON_FRACTIONS, bfs_clusters=BFS_CLUSTERS, reps: int = 1,
              device: int = 0) -> dict:
     """Best {"workers", "recon_max_ctas", "bfs_max_cluster", "mpx_s"} over the
@@ -41,6 +50,8 @@ def autotune(tiles, workers=WORKERS, recon_fractions=RECON_FRACTIONS, bfs_cluste
     sms = torch.cuda.get_device_properties(device).multi_processor_count
     maxr = max(t.shape[0] for t in tiles)
     maxc = max(t.shape[1] for t in tiles)
+    fit = max_workers(maxr, maxc, device)
+    workers = tuple(sorted({min(w, fit) for w in workers}))
     px = sum(t.shape[0] * t.shape[1] for t in tiles)
     arr, _labels = _tile_array(tiles)
     params = _lib.SegParams()
@@ -68,7 +79,7 @@ def autotune(tiles, workers=WORKERS, recon_fractions=RECON_FRACTIONS, bfs_cluste
 def main(argv=None) -> int:
     from . import synth_torch
     ap = argparse.ArgumentParser()
-    ap.add_argument("--tiles", type=int, default=32)
+    ap.add_argument("--tiles", type=int, default=96)
     ap.add_argument("--out", default="")
     a = ap.parse_args(argv)
     shapes = synth_torch.batch_shapes(256)[: a.tiles]

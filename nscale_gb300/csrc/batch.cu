@@ -236,9 +236,18 @@ int nsg_pool_create(nsg_pool **out, int max_rows, int max_cols, int workers, int
             pool_free(p);
             return r;
         }
-        // with several tiles in flight, each reconstruction takes half the
-        // SMs (measured: +9 % batched throughput on GB300)
-        if (workers > 1) w.ctx->c.recon_max_ctas = w.ctx->c.sm_count / 2 > 0 ? w.ctx->c.sm_count / 2 : 1;
+        // with several tiles in flight, each reconstruction runs on a share
+        // of the SMs, 4 x SMs / workers, between 8 CTAs and half the SMs: its
+        // CTA-time is about the same on fewer CTAs, and the other tiles get
+        // the rest (measured on GB300: 8 workers best at 76 CTAs, 16 at 38,
+        // 32 at 19)
+        if (workers > 1) {
+            const int sm = w.ctx->c.sm_count;
+            int r = 4 * sm / workers;
+            if (r > sm / 2) r = sm / 2;
+            if (r < 8) r = 8;
+            w.ctx->c.recon_max_ctas = r;
+        }
     }
     for (int k = 0; k < workers; ++k) p->w[k].th = std::thread([p, k] { p->work(k); });
     *out = p;
@@ -262,6 +271,36 @@ int nsg_pool_set_tuning(nsg_pool *p, const nsg_tuning *t) {
         if (r != NSG_SUCCESS) return r;
     }
     return NSG_SUCCESS;
+}
+
+int nsg_pool_set_timing(nsg_pool *p, int on) {
+    if (!p) return NSG_ERR_ARG;
+    std::lock_guard<std::mutex> lk(p->mu);
+    if (p->busy) return NSG_ERR_ARG;
+    for (auto &w : p->w) {
+        const int r = nsg_context_set_timing(w.ctx, on);
+        if (r != NSG_SUCCESS) return r;
+    }
+    return NSG_SUCCESS;
+}
+
+int nsg_pool_stage_times(nsg_pool *p, double *ms_out, int n, long long *calls) {
+    if (!p || !ms_out || n < 0) return NSG_ERR_ARG;
+    std::lock_guard<std::mutex> lk(p->mu);
+    if (p->busy) return NSG_ERR_ARG;
+    for (int i = 0; i < n; ++i) ms_out[i] = 0.0;
+    long long total = 0;
+    int stages = 0;
+    std::vector<double> one(n > 0 ? n : 1);
+    for (auto &w : p->w) {
+        long long k = 0;
+        stages = nsg_context_stage_times(w.ctx, one.data(), n, &k);
+        if (stages < 0) return stages;
+        for (int i = 0; i < n && i < stages; ++i) ms_out[i] += one[i];
+        total += k;
+    }
+    if (calls) *calls = total;
+    return stages;
 }
 
 int nsg_segment_nuclei_batch(nsg_pool *p, nsg_tile *tiles, int n, const nsg_seg_params *prm, int flags) {

@@ -68,8 +68,11 @@ enum Ctrl : int {
 };
 
 // Per-stage CUDA-event timing of segmentNuclei (the GPU analogue of the
-// reference's SimpleCSVLogger::logTimeSinceLastLog stage names).
-constexpr int kStages = 19;
+// reference's SimpleCSVLogger::logTimeSinceLastLog stage names).  Stages
+// 19-21 split the watershed: flood domains + P1, P2 + the BFS, P3 (the
+// "watershed" stage keeps the rest of it).
+constexpr int kStages = 22;
+constexpr int kStageWsP1 = 19, kStageWsBfs = 20, kStageWsP3 = 21;
 struct StageTimer {
     bool on = false;
     bool created = false;
@@ -103,6 +106,7 @@ struct nsg_context {
 };
 
 namespace nsg {
+void stage_mark(Ctx &c, int stage, cudaStream_t s);  // end of `stage` when timing is on
 int stain_matrix(const double *M9, const uint8_t *b3, double *Q6);
 int color_deconv_dev(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int cols, const float *Q6, uint8_t *H,
                      uint8_t *E, cudaStream_t s);

@@ -79,7 +79,8 @@ int take_counts(Ctx &c) {
 const char *kStageNames[kStages] = {"background", "RBC", "open19", "reconToNuclei", "fillHoles1",
                                    "areaThreshold1", "blobsGt45", "fillHoles2", "openBlobs", "30To1000",
                                    "dilate", "distTransform", "imhmin", "watershed", "20To1000",
-                                   "fillHolesLast", "bwlabel2", "bounding_box", "other"};
+                                   "fillHolesLast", "bwlabel2", "bounding_box", "other", "watershed_P1",
+                                   "watershed_BFS", "watershed_P3"};
 
 // timer: record the end of `stage` (the segment since the previous mark)
 void t_start(Ctx &c, cudaStream_t s) {
@@ -117,6 +118,8 @@ void t_finish(Ctx &c, cudaStream_t s) {
 }
 
 }  // namespace
+
+void stage_mark(Ctx &c, int stage, cudaStream_t s) { t_mark(c, stage, s); }
 
 int segment_nuclei_dev(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int cols, const nsg_seg_params &p,
                        int32_t *labels_out, uint8_t *mask_out, int *compcount, int32_t **bbox, cudaStream_t s) {

@@ -983,9 +983,12 @@ __device__ __forceinline__ void notify(Queue &q, int t, int bits) {
 template <typename T, int TW, int TH, int P, int NW, bool PACKED>
 using TileOf = typename std::conditional<PACKED, TileU8<TW, TH>, TileSmem<T, TW, TH, P>>::type;
 
-template <typename T, int TW, int TH, int P, int NW, bool PACKED>
-__global__ void __launch_bounds__(NW * 32, (NW >= 16 && !PACKED) ? 1 : 2) recon_cta(const T *__restrict__ mask, T *out, int rows, int cols, int conn,
-                                                 int tiles_x, int tiles_y, Queue q) {
+// MINB: CTAs per SM the register budget is sized for (8 warps: 4, i.e. at
+// most 64 registers a thread, so the reconstructions of several tiles in
+// flight can share an SM; 2 is kept as a tuning knob)
+template <typename T, int TW, int TH, int P, int NW, bool PACKED, int MINB>
+__global__ void __launch_bounds__(NW * 32, MINB) recon_cta(const T *__restrict__ mask, T *out, int rows, int cols,
+                                                           int conn, int tiles_x, int tiles_y, Queue q) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     using Sm = TileOf<T, TW, TH, P, NW, PACKED>;
     Sm &sm = *reinterpret_cast<Sm *>(sm_raw);
@@ -1032,7 +1035,7 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 16 && !PACKED) ? 1 : 2) recon_
     }
 }
 
-template <typename T, int TW, int TH, int P, int NW, bool PACKED = false>
+template <typename T, int TW, int TH, int P, int NW, bool PACKED = false, int MINB = (NW >= 16 && !PACKED) ? 1 : 2>
 int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int cols, int conn, cudaStream_t s) {
     NSG_TRY(check_dims(c, rows, cols));
     NSG_TRY(check_conn(c, conn));
@@ -1094,7 +1097,7 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
     if (const char *e = getenv("NSG_RECON_IDLE")) q.idle_limit = atoi(e);  // tuning knob
     q.stats = c.ws.ctrl + C_RSTATS;
     const size_t smem = sizeof(TileOf<T, TW, TH, P, NW, PACKED>);
-    auto kfn = recon_cta<T, TW, TH, P, NW, PACKED>;
+    auto kfn = recon_cta<T, TW, TH, P, NW, PACKED, MINB>;
     NSG_CUDA_TRY(c, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     NSG_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, NW * 32, smem));
@@ -1129,6 +1132,14 @@ int recon_warps() {
     return 8;  // more warps shorten one reconstruction but crowd out concurrent tiles
 }
 
+// register budget of the 8-warp tile CTA: sized for 4 CTAs per SM (default) or 2
+int recon_minb() {
+    if (const char *e = getenv("NSG_RECON_MINB")) {  // tuning knob: 2 or 4
+        if (atoi(e) == 2) return 2;
+    }
+    return 4;
+}
+
 }  // namespace
 
 int recon_u8(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t *out, int rows, int cols, int conn,
@@ -1140,7 +1151,10 @@ int recon_u8(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t *out, i
         if (nw == 16) return run_recon_cta<uint8_t, 128, 128, 132, 16, true>(c, marker, mask, out, rows, cols, conn, s);
         return run_recon_cta<uint8_t, 128, 128, 132, 8, true>(c, marker, mask, out, rows, cols, conn, s);
     }
-    if (nw == 8) return run_recon_cta<uint8_t, 128, 128, 132, 8>(c, marker, mask, out, rows, cols, conn, s);
+    if (nw == 8) {
+        if (recon_minb() == 2) return run_recon_cta<uint8_t, 128, 128, 132, 8, false, 2>(c, marker, mask, out, rows, cols, conn, s);
+        return run_recon_cta<uint8_t, 128, 128, 132, 8, false, 4>(c, marker, mask, out, rows, cols, conn, s);
+    }
     if (nw == 32) return run_recon_cta<uint8_t, 128, 128, 132, 32>(c, marker, mask, out, rows, cols, conn, s);
     return run_recon_cta<uint8_t, 128, 128, 132, 16>(c, marker, mask, out, rows, cols, conn, s);
 }
@@ -1148,7 +1162,10 @@ int recon_u8(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t *out, i
 int recon_f32(Ctx &c, const float *marker, const float *mask, float *out, int rows, int cols, int conn,
               cudaStream_t s) {
     const int nw = recon_warps();
-    if (nw == 8) return run_recon_cta<float, 64, 64, 67, 8>(c, marker, mask, out, rows, cols, conn, s);
+    if (nw == 8) {
+        if (recon_minb() == 2) return run_recon_cta<float, 64, 64, 67, 8, false, 2>(c, marker, mask, out, rows, cols, conn, s);
+        return run_recon_cta<float, 64, 64, 67, 8, false, 4>(c, marker, mask, out, rows, cols, conn, s);
+    }
     if (nw == 32) return run_recon_cta<float, 64, 64, 67, 32>(c, marker, mask, out, rows, cols, conn, s);
     return run_recon_cta<float, 64, 64, 67, 16>(c, marker, mask, out, rows, cols, conn, s);
 }

@@ -1381,6 +1381,7 @@ int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int 
     k_phase1<<<gd, 64, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
+    stage_mark(c, kStageWsP1, s);
     // P2
     k_true_dummies<<<g, kB, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
@@ -1399,6 +1400,7 @@ int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int 
     NSG_COUNT_LAUNCH();
     NSG_TRY(launch_bfs(c, a, a.fgimg, s));
     NSG_LAUNCH_CHECK(c);
+    stage_mark(c, kStageWsBfs, s);
     k_shells<<<g, kB, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
     uint8_t *pimg = a.fgimg;  // reuse: the domain image is no longer needed
@@ -1428,6 +1430,7 @@ int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int 
     NSG_LAUNCH_CHECK(c);
     k_phase3<<<gd, 64, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
+    stage_mark(c, kStageWsP3, s);
     k_assemble<<<g, kB, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);

@@ -57,6 +57,18 @@ class TilePool:
         t = _lib.Tuning(recon_max_ctas, bfs_max_cluster)
         _check(self.L.nsg_pool_set_tuning(self.h, C.byref(t)), "nsg_pool_set_tuning")
 
+    def set_timing(self, on: bool = True) -> None:
+        """nsg_pool_set_timing: per-stage CUDA-event timing on every worker (resets the sums)."""
+        _check(self.L.nsg_pool_set_timing(self.h, 1 if on else 0), "nsg_pool_set_timing")
+
+    def stage_times(self) -> tuple[dict, int]:
+        """nsg_pool_stage_times: ({stage name: ms summed over workers}, tiles timed)."""
+        ms = (C.c_double * 32)()
+        calls = C.c_longlong(0)
+        n = self.L.nsg_pool_stage_times(self.h, ms, 32, C.byref(calls))
+        _check(n, "nsg_pool_stage_times")
+        return {self.L.nsg_stage_name(i).decode(): ms[i] for i in range(n)}, calls.value
+
     def run(self, tiles: "C.Array", params: _lib.SegParams | None = None, host: bool = False) -> int:
         """nsg_segment_nuclei_batch over a prepared ctypes array of Tile."""
         rc = self.L.nsg_segment_nuclei_batch(self.h, tiles, len(tiles), C.byref(params) if params else None,

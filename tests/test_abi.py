@@ -68,3 +68,5 @@ def test_pool_and_server_host_checks(nsg):
     t = _lib.Tuning(0, 0)
     assert nsg.nsg_context_set_tuning(None, C.byref(t)) == _lib.ERR_ARG
     assert nsg.nsg_pool_set_tuning(None, C.byref(t)) == _lib.ERR_ARG
+    assert nsg.nsg_pool_set_timing(None, 1) == _lib.ERR_ARG
+    assert nsg.nsg_pool_stage_times(None, None, 0, None) == _lib.ERR_ARG

@@ -148,9 +148,15 @@ def test_tuning_changes_no_result(cuda):
     try:
         base = pool.segment(tiles)
         pool.set_tuning(recon_max_ctas=7, bfs_max_cluster=2)
+        pool.set_timing(True)
         tuned = pool.segment(tiles)
+        stages, timed = pool.stage_times()
+        pool.set_timing(False)
     finally:
         pool.close()
     for (s0, l0, n0, b0), (s1, l1, n1, b1) in zip(base, tuned):
         assert s0 == s1 and n0 == n1
         assert torch.equal(l0, l1) and np.array_equal(b0, b1)
+    # per-stage timing of the pool's workers: every tile timed, the heavy stages seen
+    assert timed == len(tiles)
+    assert stages["reconToNuclei"] > 0 and stages["watershed"] > 0
