@@ -18,8 +18,8 @@ import torch
 from . import _lib
 from .serving import TilePool
 
-WORKERS = (16, 24, 32)
-RECON_FRACTIONS = (1 / 16, 1 / 8, 1 / 4)
+WORKERS = (24, 32, 40)
+RECON_FRACTIONS = (1 / 32, 1 / 16, 1 / 8)
 BFS_CLUSTERS = (16,)
 
 

@@ -237,15 +237,15 @@ int nsg_pool_create(nsg_pool **out, int max_rows, int max_cols, int workers, int
             return r;
         }
         // with several tiles in flight, each reconstruction runs on a share
-        // of the SMs, 4 x SMs / workers, between 8 CTAs and half the SMs: its
+        // of the SMs, 2 x SMs / workers, between 4 CTAs and half the SMs: its
         // CTA-time is about the same on fewer CTAs, and the other tiles get
-        // the rest (measured on GB300: 8 workers best at 76 CTAs, 16 at 38,
-        // 32 at 19)
+        // the rest (measured on GB300 with 32 workers: 9 CTAs 882 Mpixel/s,
+        // 19 815, 38 765)
         if (workers > 1) {
             const int sm = w.ctx->c.sm_count;
-            int r = 4 * sm / workers;
+            int r = 2 * sm / workers;
             if (r > sm / 2) r = sm / 2;
-            if (r < 8) r = 8;
+            if (r < 4) r = 4;
             w.ctx->c.recon_max_ctas = r;
         }
     }

@@ -351,7 +351,7 @@ __device__ int q_finish(Queue &q, int t) {
 template <typename T, int TW, int TH, int P>
 struct TileSmem {
     T o[(TH + 2) * P];                         // the tile and its halo (row pitch P)
-    T m[TH * TW];                              // the mask
+    T m[TH * P];                               // the mask (row pitch P: a thread per row reads it without bank conflicts)
     T eN[TW], eS[TW], eW[TH], eE[TH];          // the tile's edge values when it was loaded
     T mN[TW + 2], mS[TW + 2], mW[TH], mE[TH];  // the mask just outside the tile (neighbours' pixels)
     unsigned drow[TH / 32], dcol[TW / 32];     // dirty rows / columns
@@ -442,12 +442,140 @@ __device__ __forceinline__ void line_scan(T (&lo)[K], T (&hi)[K], T first, T las
     }
 }
 
+// ---- one line per lane ---------------------------------------------------------
+// When many lines of a 32-line group are dirty, each lane scans one whole line
+// of the group itself: the raster step then the anti-raster step, pixel by
+// pixel, with the cross-line neighbours kept in a sliding window.  About a
+// quarter of the instructions of the shuffle scan per line; a group with few
+// dirty lines keeps the shuffle scan (a lane-per-line pass costs the same
+// whether 1 or 32 of its lines are dirty).  uint8 only: a pixel outside the
+// image has mask 0, so min/max alone keep it 0.
+constexpr int kSeqMinLines = 8;  // dirty lines of a group from which lanes scan one line each
+
+// Row r (tile coordinates) of the tile in `o` (pitch P, one-pixel halo), mask
+// row `m`.  chg[j] bit k: pixel j * 32 + k changed.
+template <int TW, int P>
+__device__ __forceinline__ void row_seq(uint8_t *o, const uint8_t *m, int r, bool conn8, unsigned (&chg)[TW / 32]) {
+    uint8_t *row = o + (r + 1) * P + 1;
+    const uint8_t *up = row - P, *dn = row + P;
+    uint8_t prev = row[-1];
+    uint8_t ul = up[-1], uc = up[0], dl = dn[-1], dc = dn[0];
+#pragma unroll 1
+    for (int j = 0; j < TW / 32; ++j) {
+        unsigned bits = 0;
+#pragma unroll 8
+        for (int k = 0; k < 32; ++k) {
+            const int x = j * 32 + k;
+            const uint8_t ur = up[x + 1], dr = dn[x + 1], cur = row[x], mk = m[x];
+            uint8_t w8 = smax(cur, smax(uc, dc));
+            if (conn8) w8 = smax(w8, smax(smax(ul, ur), smax(dl, dr)));
+            const uint8_t v = clampv(prev, smin(w8, mk), mk);
+            if (v != cur) {
+                row[x] = v;
+                bits |= 1u << k;
+            }
+            prev = v;
+            ul = uc;
+            uc = ur;
+            dl = dc;
+            dc = dr;
+        }
+        chg[j] = bits;
+    }
+    uint8_t nxt = row[TW];
+#pragma unroll 1
+    for (int j = TW / 32 - 1; j >= 0; --j) {
+        unsigned bits = 0;
+#pragma unroll 8
+        for (int k = 31; k >= 0; --k) {
+            const int x = j * 32 + k;
+            const uint8_t f = row[x];
+            const uint8_t v = clampv(nxt, f, m[x]);
+            if (v != f) {
+                row[x] = v;
+                bits |= 1u << k;
+            }
+            nxt = v;
+        }
+        chg[j] |= bits;
+    }
+}
+
+// Column c of the tile; chg[j] bit k: pixel of row j * 32 + k changed.
+template <int TH, int P>
+__device__ __forceinline__ void col_seq(uint8_t *o, const uint8_t *m, int c, bool conn8, unsigned (&chg)[TH / 32]) {
+    uint8_t *col = o + P + c + 1;  // pixel (0, c)
+    const uint8_t *mc = m + c;
+    uint8_t prev = col[-P];
+    uint8_t lp = col[-P - 1], rp = col[-P + 1], lc = col[-1], rc = col[1];
+#pragma unroll 1
+    for (int j = 0; j < TH / 32; ++j) {
+        unsigned bits = 0;
+#pragma unroll 8
+        for (int k = 0; k < 32; ++k) {
+            const int y = j * 32 + k;
+            uint8_t *px = col + y * P;
+            const uint8_t ln = px[P - 1], rn = px[P + 1], cur = px[0], mk = mc[y * P];
+            uint8_t w8 = smax(cur, smax(lc, rc));
+            if (conn8) w8 = smax(w8, smax(smax(lp, rp), smax(ln, rn)));
+            const uint8_t v = clampv(prev, smin(w8, mk), mk);
+            if (v != cur) {
+                px[0] = v;
+                bits |= 1u << k;
+            }
+            prev = v;
+            lp = lc;
+            rp = rc;
+            lc = ln;
+            rc = rn;
+        }
+        chg[j] = bits;
+    }
+    uint8_t nxt = col[TH * P];
+#pragma unroll 1
+    for (int j = TH / 32 - 1; j >= 0; --j) {
+        unsigned bits = 0;
+#pragma unroll 8
+        for (int k = 31; k >= 0; --k) {
+            const int y = j * 32 + k;
+            uint8_t *px = col + y * P;
+            const uint8_t f = px[0];
+            const uint8_t v = clampv(nxt, f, mc[y * P]);
+            if (v != f) {
+                px[0] = v;
+                bits |= 1u << k;
+            }
+            nxt = v;
+        }
+        chg[j] |= bits;
+    }
+}
+
+// Whole warp: every lane changed the pixels chg[] of one line; mark the
+// perpendicular lines they lie on and the ones beside them in `m` (N lines).
+template <int N>
+__device__ __forceinline__ void mark_dirty_seq(unsigned *m, const unsigned (&chg)[N / 32]) {
+    const int lane = threadIdx.x & 31;
+    unsigned w[N / 32];
+#pragma unroll
+    for (int j = 0; j < N / 32; ++j) w[j] = __reduce_or_sync(0xffffffffu, chg[j]);
+#pragma unroll
+    for (int j = 0; j < N / 32; ++j) {
+        unsigned d = w[j] | (w[j] << 1) | (w[j] >> 1);
+        if (j > 0) d |= w[j - 1] >> 31;
+        if (j + 1 < N / 32) d |= w[j + 1] << 31;
+        if (lane == j && d) atomicOr(&m[j], d);
+    }
+}
+
 // One pass over tile (tx, ty): load, alternate row / column phases over the
 // dirty lines until nothing changes, report which neighbours must run again,
 // write back.
-template <typename T, int TW, int TH, int P, int NW>
+template <typename T, int TW, int TH, int P, int NW, bool HYB = false>
 __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, int cols, bool conn8, int tx, int ty,
                                  int dirty_in, TileSmem<T, TW, TH, P> &sm) {
+    static_assert(!HYB || (std::is_same<T, uint8_t>::value && NW == TH / 32 && NW == TW / 32),
+                  "lane-per-line scans: uint8, one warp per 32-line group");
     constexpr int KX = TW / 32, KY = TH / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int y0 = ty * TH, x0 = tx * TW;
@@ -461,7 +589,7 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
     for (int i = threadIdx.x; i < TH * TW; i += NW * 32) {
         int r = i / TW, cc = i - r * TW;
         int y = y0 + r, x = x0 + cc;
-        sm.m[i] = (y < rows && x < cols) ? __ldg(mask + (int64_t)y * cols + x) : (T)0;
+        sm.m[r * P + cc] = (y < rows && x < cols) ? __ldg(mask + (int64_t)y * cols + x) : (T)0;
     }
     auto mask_at = [&](int y, int x) -> T {
         return (y >= 0 && y < rows && x >= 0 && x < cols) ? __ldg(mask + (int64_t)y * cols + x) : (T)0;
@@ -520,6 +648,23 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
 #pragma unroll
         for (int w = 0; w < TH / 32; ++w) {
             unsigned bits = rm[w];
+            if constexpr (HYB) {
+                if (__popc(bits) >= kSeqMinLines) {
+                    if (warp == w) {
+                        unsigned chg[TW / 32] = {};
+                        const int r = w * 32 + lane;
+                        if ((bits >> lane) & 1u) row_seq<TW, P>(o, sm.m + r * P, r, conn8, chg);
+                        unsigned any = 0;
+#pragma unroll
+                        for (int j = 0; j < TW / 32; ++j) any |= chg[j];
+                        if (__any_sync(0xffffffffu, any != 0)) {
+                            chr = true;
+                            mark_dirty_seq<TW>(sm.dcol, chg);
+                        }
+                    }
+                    continue;
+                }
+            }
             while (bits) {
                 const int r = w * 32 + __ffs(bits) - 1;
                 bits &= bits - 1;
@@ -533,7 +678,7 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
                     cur[k] = row[x];
                     T w8 = smax(cur[k], smax(up[x], dn[x]));
                     if (conn8) w8 = smax(w8, smax(smax(up[x - 1], up[x + 1]), smax(dn[x - 1], dn[x + 1])));
-                    T mk = sm.m[r * TW + x];
+                    T mk = sm.m[r * P + x];
                     bool in = r < vr && x < vc;
                     lo[k] = in ? smin(w8, mk) : (T)0;
                     hi[k] = in ? mk : (T)0;
@@ -568,6 +713,22 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
 #pragma unroll
         for (int w = 0; w < TW / 32; ++w) {
             unsigned bits = cm[w];
+            if constexpr (HYB) {
+                if (__popc(bits) >= kSeqMinLines) {
+                    if (warp == w) {
+                        unsigned chg[TH / 32] = {};
+                        if ((bits >> lane) & 1u) col_seq<TH, P>(o, sm.m, w * 32 + lane, conn8, chg);
+                        unsigned any = 0;
+#pragma unroll
+                        for (int j = 0; j < TH / 32; ++j) any |= chg[j];
+                        if (__any_sync(0xffffffffu, any != 0)) {
+                            chc = true;
+                            mark_dirty_seq<TH>(sm.drow, chg);
+                        }
+                    }
+                    continue;
+                }
+            }
             while (bits) {
                 const int cidx = w * 32 + __ffs(bits) - 1;
                 bits &= bits - 1;
@@ -580,7 +741,7 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
                     cur[k] = p[0];
                     T w8 = smax(cur[k], smax(p[-1], p[1]));
                     if (conn8) w8 = smax(w8, smax(smax(p[-P - 1], p[-P + 1]), smax(p[P - 1], p[P + 1])));
-                    T mk = sm.m[y * TW + cidx];
+                    T mk = sm.m[y * P + cidx];
                     bool in = y < vr && cidx < vc;
                     lo[k] = in ? smin(w8, mk) : (T)0;
                     hi[k] = in ? mk : (T)0;
@@ -986,7 +1147,7 @@ using TileOf = typename std::conditional<PACKED, TileU8<TW, TH>, TileSmem<T, TW,
 // MINB: CTAs per SM the register budget is sized for (8 warps: 4, i.e. at
 // most 64 registers a thread, so the reconstructions of several tiles in
 // flight can share an SM; 2 is kept as a tuning knob)
-template <typename T, int TW, int TH, int P, int NW, bool PACKED, int MINB>
+template <typename T, int TW, int TH, int P, int NW, bool PACKED, int MINB, bool HYB>
 __global__ void __launch_bounds__(NW * 32, MINB) recon_cta(const T *__restrict__ mask, T *out, int rows, int cols,
                                                            int conn, int tiles_x, int tiles_y, Queue q) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
@@ -1008,7 +1169,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) recon_cta(const T *__restrict__
             if constexpr (PACKED)
                 cta_process_tile_u8<TW, TH, NW>(mask, out, rows, cols, conn8, tx, ty, dirty, sm);
             else
-                cta_process_tile<T, TW, TH, P, NW>(mask, out, rows, cols, conn8, tx, ty, dirty, sm);
+                cta_process_tile<T, TW, TH, P, NW, HYB>(mask, out, rows, cols, conn8, tx, ty, dirty, sm);
             if (threadIdx.x == 0) {
                 const unsigned edges = (unsigned)sm.edges;
                 // our top edge is the upper tile's bottom halo, and so on
@@ -1035,7 +1196,8 @@ __global__ void __launch_bounds__(NW * 32, MINB) recon_cta(const T *__restrict__
     }
 }
 
-template <typename T, int TW, int TH, int P, int NW, bool PACKED = false, int MINB = (NW >= 16 && !PACKED) ? 1 : 2>
+template <typename T, int TW, int TH, int P, int NW, bool PACKED = false, int MINB = (NW >= 16 && !PACKED) ? 1 : 2,
+          bool HYB = false>
 int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int cols, int conn, cudaStream_t s) {
     NSG_TRY(check_dims(c, rows, cols));
     NSG_TRY(check_conn(c, conn));
@@ -1097,13 +1259,15 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
     if (const char *e = getenv("NSG_RECON_IDLE")) q.idle_limit = atoi(e);  // tuning knob
     q.stats = c.ws.ctrl + C_RSTATS;
     const size_t smem = sizeof(TileOf<T, TW, TH, P, NW, PACKED>);
-    auto kfn = recon_cta<T, TW, TH, P, NW, PACKED, MINB>;
+    auto kfn = recon_cta<T, TW, TH, P, NW, PACKED, MINB, HYB>;
     NSG_CUDA_TRY(c, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     NSG_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, NW * 32, smem));
-    // One CTA per SM by default: the work is CTA-throughput bound and a second
-    // CTA per SM mostly takes room that concurrent streams' kernels can use.
-    int want = 1;
+    // One CTA per SM by default (two for the 4-warp lane-per-line form): the
+    // work is CTA-throughput bound and more CTAs per SM mostly take room that
+    // concurrent streams' kernels can use (measured on one 4096^2 tile, 4
+    // warps: 1 CTA per SM 12.2 ms, 2 9.6 ms, 4 12.5 ms).
+    int want = HYB ? 2 : 1;
     if (const char *e = getenv("NSG_RECON_CTAS_PER_SM")) want = atoi(e);  // tuning knob
     if (want >= 1 && want < per_sm) per_sm = want;
     if (per_sm < 1) per_sm = 1;
@@ -1151,6 +1315,10 @@ int recon_u8(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t *out, i
         if (nw == 16) return run_recon_cta<uint8_t, 128, 128, 132, 16, true>(c, marker, mask, out, rows, cols, conn, s);
         return run_recon_cta<uint8_t, 128, 128, 132, 8, true>(c, marker, mask, out, rows, cols, conn, s);
     }
+    bool hyb = true;  // lane-per-line scans for dense line groups, 4 warps (tuning knob NSG_RECON_HYB=0: shuffle scans only)
+    if (const char *e = getenv("NSG_RECON_HYB")) hyb = atoi(e) != 0;
+    if (hyb && !getenv("NSG_RECON_WARPS"))
+        return run_recon_cta<uint8_t, 128, 128, 132, 4, false, 4, true>(c, marker, mask, out, rows, cols, conn, s);
     if (nw == 8) {
         if (recon_minb() == 2) return run_recon_cta<uint8_t, 128, 128, 132, 8, false, 2>(c, marker, mask, out, rows, cols, conn, s);
         return run_recon_cta<uint8_t, 128, 128, 132, 8, false, 4>(c, marker, mask, out, rows, cols, conn, s);
