@@ -99,7 +99,28 @@ struct PW {
     int *dsize, *doff, *bbx0, *bbx1, *bby0, *bby1, *npop, *cut, *sup, *mcount, *moff, *mfill, *mlist, *icount,
         *ioff, *ifill, *ilist, *cand, *pend, *pend2;
     unsigned long long *dfirst;
+    int *grp;  // P3: flood group owning each pixel, -1 none (aliases the BFS frontier, free by then)
 };
+
+// A pop's reads, issued together: the four neighbours' flags, markers,
+// labels and colours (and, in P3, states and groups) do not depend on one
+// another, so one memory round trip serves the pop instead of a chain of
+// dependent loads.  Labels are the only ones the flood writes; a pop writes
+// its own pixel and the neighbours it queues, each once, after reading them.
+struct Nb4 {
+    uint8_t f[4];
+    int mk[4], lab[4];
+    uint32_t col[4];
+};
+__device__ __forceinline__ void load_nb(const PW &a, const int (&nb)[4], Nb4 &o) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        o.f[k] = __ldg((const unsigned char *)a.flags + nb[k]);
+        o.mk[k] = __ldg(a.mk + nb[k]);
+        o.lab[k] = a.lab[nb[k]];
+        o.col[k] = __ldg(a.col + nb[k]);
+    }
+}
 
 __device__ __forceinline__ int cdiff(uint32_t a, uint32_t b) {
     int db = abs((int)(a & 255) - (int)(b & 255));
@@ -257,6 +278,10 @@ __device__ void phase1_domain(const PW &a, int d) {
         }
         seq++;
         const int p = e;
+        const int nb[4] = {p - 1, p + 1, p - W, p + W};
+        Nb4 nv;
+        load_nb(a, nb, nv);
+        const uint32_t c = __ldg(a.col + p);
         int top = lv >= runmax;
         if (top) {
             runmax = lv;
@@ -267,16 +292,14 @@ __device__ void phase1_domain(const PW &a, int d) {
         a.rlocal[p] = local;
         a.popl[base + local] = p;
         local++;
-        const int nb[4] = {p - 1, p + 1, p - W, p + W};
         int lb = 0;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            int qq = nb[k];
-            uint8_t fq = a.flags[qq];
+            const uint8_t fq = nv.f[k];
             int t = 0;
             if (fq & F_BORDER) continue;
-            if (!(fq & F_UNK)) t = a.mk[qq];
-            else if (fq & F_FG) t = a.lab[qq];
+            if (!(fq & F_UNK)) t = nv.mk[k];
+            else if (fq & F_FG) t = nv.lab[k];
             if (t > 0) {
                 if (lb == 0) lb = t;
                 else if (t != lb) lb = WSHED;
@@ -287,11 +310,10 @@ __device__ void phase1_domain(const PW &a, int d) {
             if (lb == 0) set_fallback(a, 9);
             continue;
         }
-        const uint32_t c = a.col[p];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             int qq = nb[k];
-            uint8_t fq = a.flags[qq];
+            const uint8_t fq = nv.f[k];
             if (!(fq & F_UNK)) continue;
             if (fq & F_U) {
                 if (fq & F_INIT) continue;  // queued from the start
@@ -314,7 +336,7 @@ __device__ void phase1_domain(const PW &a, int d) {
                 a.dpix[kk] = qq;
                 a.ddom[kk] = d;
                 a.rparent[id] = p;
-                a.rmeta[id] = cdiff(c, a.col[qq]) | (k << 9);
+                a.rmeta[id] = cdiff(c, nv.col[k]) | (k << 9);
                 a.rlocal[id] = -1;
                 a.dnextu[kk] = atomicExch(a.utrue + qq, id);
                 int l2 = m_level(a.rmeta[id]);
@@ -322,8 +344,8 @@ __device__ void phase1_domain(const PW &a, int d) {
                 if (l2 < active) active = l2;
                 continue;
             }
-            if (a.lab[qq] != 0) continue;
-            int l2 = cdiff(c, a.col[qq]);
+            if (nv.lab[k] != 0) continue;
+            int l2 = cdiff(c, nv.col[k]);
             a.rparent[qq] = p;
             a.rmeta[qq] = l2 | (k << 9);
             q_push(q, a.next, l2, qq);
@@ -843,21 +865,26 @@ __global__ void k_inj_count(PW a, int pass) {
         else a.ilist[a.ioff[r] + atomicAdd(a.ifill + r, 1)] = p;
     }
 }
+// the flood group owning each pixel (the owned() test of P3, precomputed)
+__global__ void k_pixel_groups(PW a) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
+        const uint8_t f = a.flags[p];
+        int g = -1;
+        if (f & F_FG) {
+            g = a.sup[a.dom[p]];
+        } else if (f & F_U) {
+            const int o = a.uown[p];
+            if (o >= 0 && (a.st[p] & (S_ACTIVE | S_POCKET))) g = a.sup[o];
+        }
+        a.grp[p] = g;
+    }
+}
 __global__ void k_reset_owned_u(PW a) {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x)
         if ((a.st[p] & (S_ACTIVE | S_POCKET)) && a.uown[p] >= 0) a.lab[p] = 0;
 }
 
 // ---------------------------------------------------------------- P3 --------
-__device__ __forceinline__ bool owned(const PW &a, int q, int S) {
-    uint8_t f = a.flags[q];
-    if (f & F_FG) return a.sup[a.dom[q]] == S;
-    if (f & F_U) {
-        int o = a.uown[q];
-        return o >= 0 && (a.st[q] & (S_ACTIVE | S_POCKET)) && a.sup[o] == S;
-    }
-    return false;
-}
 
 // replay domain d up to its T_e state (pre-T_e rules)
 __device__ bool replay(const PW &a, int d, Q &q, int &active) {
@@ -883,17 +910,20 @@ __device__ bool replay(const PW &a, int d, Q &q, int &active) {
         q.h[active] = a.next[e];
         if (q.h[active] < 0) q.t[active] = -1;
         const int p = e;
-        if (!(a.flags[p] & F_FG)) return false;  // no U pop before T_e
-        ++local;
         const int nb[4] = {p - 1, p + 1, p - W, p + W};
+        Nb4 nv;
+        load_nb(a, nb, nv);
+        const uint32_t c = __ldg(a.col + p);
+        if (!(__ldg((const unsigned char *)a.flags + p) & F_FG)) return false;  // no U pop before T_e
+        ++local;
         int lb = 0;
+#pragma unroll
         for (int k = 0; k < 4; ++k) {
-            int qq = nb[k];
-            uint8_t fq = a.flags[qq];
+            const uint8_t fq = nv.f[k];
             int t = 0;
             if (fq & F_BORDER) continue;
-            if (!(fq & F_UNK)) t = a.mk[qq];
-            else if (fq & F_FG) t = a.lab[qq];
+            if (!(fq & F_UNK)) t = nv.mk[k];
+            else if (fq & F_FG) t = nv.lab[k];
             if (t > 0) {
                 if (lb == 0) lb = t;
                 else if (t != lb) lb = WSHED;
@@ -902,17 +932,17 @@ __device__ bool replay(const PW &a, int d, Q &q, int &active) {
         a.lab[p] = lb;
         if (lb == 0) return false;
         if (lb == WSHED) continue;
-        const uint32_t c = a.col[p];
+#pragma unroll
         for (int k = 0; k < 4; ++k) {
             int qq = nb[k];
-            uint8_t fq = a.flags[qq];
+            const uint8_t fq = nv.f[k];
             if (!(fq & F_UNK)) continue;
             if (fq & F_U) {
                 if (!(a.st[qq] & S_ACTIVE)) continue;
                 int te = a.utrue[qq];
                 if (te < a.n || a.ddom[te - a.n] != d) continue;
-                if (a.lab[qq] != 0) continue;
-                int l2 = cdiff(c, a.col[qq]);
+                if (nv.lab[k] != 0) continue;
+                int l2 = cdiff(c, nv.col[k]);
                 a.rparent[qq] = p;
                 a.rmeta[qq] = l2 | (k << 9);
                 q_push(q, a.next, l2, qq);
@@ -920,8 +950,8 @@ __device__ bool replay(const PW &a, int d, Q &q, int &active) {
                 a.lab[qq] = IN_QUEUE;
                 continue;
             }
-            if (a.lab[qq] != 0) continue;
-            int l2 = cdiff(c, a.col[qq]);
+            if (nv.lab[k] != 0) continue;
+            int l2 = cdiff(c, nv.col[k]);
             q_push(q, a.next, l2, qq);
             if (l2 < active) active = l2;
             a.lab[qq] = IN_QUEUE;
@@ -1029,15 +1059,25 @@ __device__ void phase3_group(const PW &a, int S) {
         if (q.h[active] < 0) q.t[active] = -1;
         const int p = e;
         const int nb[4] = {p - 1, p + 1, p - W, p + W};
-        int lb = 0;
+        Nb4 nv;
+        load_nb(a, nb, nv);
+        uint8_t sq[4];
+        int gq[4];
+#pragma unroll
         for (int k = 0; k < 4; ++k) {
-            int qq = nb[k];
-            uint8_t fq = a.flags[qq];
+            sq[k] = __ldg((const unsigned char *)a.st + nb[k]);
+            gq[k] = __ldg(a.grp + nb[k]);
+        }
+        const uint32_t c = __ldg(a.col + p);
+        int lb = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint8_t fq = nv.f[k];
             int t = 0;
             if (fq & F_BORDER) continue;
-            if (!(fq & F_UNK)) t = a.mk[qq];
-            else if (a.st[qq] & S_R) t = X;
-            else if (owned(a, qq, S)) t = a.lab[qq];
+            if (!(fq & F_UNK)) t = nv.mk[k];
+            else if (sq[k] & S_R) t = X;
+            else if (gq[k] == S) t = nv.lab[k];
             if (t > 0) {
                 if (lb == 0) lb = t;
                 else if (t != lb) lb = WSHED;
@@ -1049,19 +1089,18 @@ __device__ void phase3_group(const PW &a, int S) {
             return;
         }
         if (lb == WSHED) continue;
-        const uint32_t c = a.col[p];
+#pragma unroll
         for (int k = 0; k < 4; ++k) {
             int qq = nb[k];
-            uint8_t fq = a.flags[qq];
+            const uint8_t fq = nv.f[k];
             if (!(fq & F_UNK)) continue;
-            uint8_t sq = a.st[qq];
-            if (sq & (S_R | S_CERTAIN)) continue;
-            if (!owned(a, qq, S)) {
+            if (sq[k] & (S_R | S_CERTAIN)) continue;
+            if (gq[k] != S) {
                 set_fallback(a, 5);
                 return;
             }
-            if (a.lab[qq] != 0) continue;
-            int l2 = cdiff(c, a.col[qq]);
+            if (nv.lab[k] != 0) continue;
+            int l2 = cdiff(c, nv.col[k]);
             q_push(q, a.next, l2, qq);
             if (l2 < active) active = l2;
             a.lab[qq] = IN_QUEUE;
@@ -1242,6 +1281,7 @@ void carve(PW &a, char *base, size_t *used_out) {
     a.proot = cv.take<int>(n);
     a.fr0 = cv.take<int>(2 * n);  // BFS frontier entries: pixel | neighbour classes << 32
     a.fr1 = cv.take<int>(2 * n);
+    a.grp = a.fr0;  // the BFS frontier is no longer needed when P3 runs
     a.popl = cv.take<int>(n);
     a.isroot = cv.take<int>(n);
     a.rank = cv.take<int>(n);
@@ -1426,6 +1466,8 @@ int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int 
     k_inj_count<<<g, kB, 0, s>>>(a, 1);
     NSG_COUNT_LAUNCH();
     k_reset_owned_u<<<g, kB, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
+    k_pixel_groups<<<g, kB, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     k_phase3<<<gd, 64, 0, s>>>(a);
