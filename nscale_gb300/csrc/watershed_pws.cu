@@ -590,55 +590,71 @@ __global__ void k_bfs_prep(PW a, uint8_t *nbm) {
     }
 }
 
-// FIFO BFS from e over black unknown pixels that are not queued at T_e.  The
-// pop rank of an R pixel is its position in the frontier sequence; a pixel
-// joins the next frontier through the earliest frontier pixel that touches
-// it, in the order (frontier position, direction).  Claims use the key
-// rank * 4 + direction with atomicMin: keys grow from layer to layer, so a
-// pixel claimed in an earlier layer keeps its key and is never taken again,
-// and the smallest key of a layer is its FIFO owner.  Every fg neighbour that
-// is neither popped nor queued at T_e records the smallest key that touches
-// it: the order in which R pushes it.
+// FIFO BFS from e over black unknown pixels that are not queued at T_e.  A
+// pixel joins the next frontier through the earliest frontier pixel that
+// touches it, in the order (frontier position, direction).  Claims use
+// atomicMin with the key 4 * key(entry) + direction, where key(entry) grows
+// with the entry's frontier position and from layer to layer, so a pixel
+// claimed in an earlier layer keeps its key and is never taken again, and the
+// smallest key of a layer is its FIFO owner.  Every fg neighbour that is
+// neither popped nor queued at T_e records the smallest key that touches it:
+// the order in which R pushes it (keys are only compared, never decoded).
 //
 // One thread-block cluster runs the BFS (up to 16 small CTAs, so that other
-// streams' kernels keep the rest of each SM).  A layer is split into
-// contiguous chunks, one per CTA, staged in shared memory; after the claims a cluster
-// barrier, then each CTA compacts its winners in order into its own segment
-// of the next frontier and publishes their count in shared memory; after a
-// second barrier every CTA reads all counts (each CTA pushed its count into
-// every CTA's shared memory) to place the segments.  Chunks are contiguous and ordered by CTA, so the next
-// frontier in global order is the concatenation of the segments.
+// streams' kernels keep the rest of each SM), one cluster barrier per layer.
+// After the barrier every CTA knows every CTA's entry count of the current
+// frontier (each CTA pushed its count into all CTAs' shared memory) and takes
+// an equal contiguous chunk of it; the claims of the whole frontier are
+// complete, so it reads the claims of its chunk's candidates, compacts its
+// winners in order into its own segment of the next frontier, and at once
+// issues the winners' claims.  A winner's key needs no other CTA's count: it
+// is its slot, base + segment * capacity + position, which orders entries as
+// their frontier positions do (segments follow chunk order) and exceeds every
+// key of the layer before (base grows by the layer's whole slot range).
+// Counts are double-buffered by layer parity, so a CTA that runs ahead into
+// the next layer never overwrites counts another CTA has yet to read.
 constexpr int kBfsThreads = 256, kBfsCtaItems = 4096, kBfsMaxCluster = 16;
-constexpr int kBfsPerThread = kBfsCtaItems / kBfsThreads;  // <= 16: 64 claim bits per thread
 
 __global__ void __launch_bounds__(kBfsThreads) k_bfs(PW a, const uint8_t *__restrict__ nbm) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
     const int C = (int)cl.num_blocks(), me = (int)cl.block_rank();
     __shared__ int sh[40];
-    __shared__ int tots[kBfsMaxCluster];      // winners of every CTA in the last layer (pushed by each CTA)
-    __shared__ int offs[kBfsMaxCluster + 1];  // where each CTA's segment starts in global order
+    __shared__ int tots[2][kBfsMaxCluster];   // entries of every CTA's segment, by layer parity
+    __shared__ int offs[kBfsMaxCluster + 1];  // where each CTA's segment starts in frontier order
     __shared__ int s_r[kBfsCtaItems];         // this CTA's chunk of the frontier
     __shared__ uint8_t s_m[kBfsCtaItems];     // and the chunk's neighbour classes
     __shared__ uint8_t s_nm[kBfsCtaItems * 4];  // neighbour classes of the pixels this CTA wins
     const bool on = a.ctl[W_EVENT] && !a.ctl[W_FALLBACK];
     const int W = a.W;
+    const int off[4] = {-1, 1, -W, W};
     // frontier entries carry their pixel's neighbour classes (one load less per layer)
     unsigned long long *Fc = reinterpret_cast<unsigned long long *>(a.fr0);
     unsigned long long *Fn = reinterpret_cast<unsigned long long *>(a.fr1);
-    if (threadIdx.x < kBfsMaxCluster) tots[threadIdx.x] = threadIdx.x == 0 ? 1 : 0;
-    if (threadIdx.x == 0 && me == 0 && on) {
+    if (threadIdx.x < kBfsMaxCluster) tots[0][threadIdx.x] = threadIdx.x == 0 ? 1 : 0;
+    if (threadIdx.x == 0 && me == 0 && on) {  // the seed: key 0, its claims before the first barrier
         const int ep = a.ctl[W_EP];
-        Fc[0] = (unsigned)ep | ((unsigned long long)nbm[ep] << 32);
+        const unsigned m = nbm[ep];
+        Fc[0] = (unsigned)ep | ((unsigned long long)m << 32);
+        for (int k = 0; k < 4; ++k) {
+            if (m & (1u << k)) atomicMin(a.claim + ep + off[k], k);
+            if (m & (16u << k)) atomicMin(a.inj + ep + off[k], k);
+        }
     }
-    cl.sync();  // every CTA has read the control flags before anything can change them
-    if (!on) return;
-    const int off[4] = {-1, 1, -W, W};
-    int prevcap = 1, base = 0, layer = 0;
-    for (;;) {
-        if (threadIdx.x < 32) {  // every CTA's count (local copies), then a warp scan
+    long long base = 0;  // key of slot 0 of the current frontier
+    int prevcap = 1;     // slots per segment of the current frontier
+    int layer = 0;
+    if (!on) {
+        cl.sync();
+        return;
+    }
+    constexpr long long kKeyLimit = (INT_MAX - 4) / 4;
+    for (;; ++layer) {
+        cl.sync();  // the frontier, its counts and its claims are complete
+        const int par = layer & 1;
+        if (threadIdx.x < 32) {  // every CTA's count, then a warp scan
             const int lane = threadIdx.x;
-            const int v = lane < C ? tots[lane] : 0;
+            const int v = lane < C ? tots[par][lane] : 0;
             int x = v;
 #pragma unroll
             for (int d = 1; d < 32; d <<= 1) {
@@ -652,7 +668,9 @@ __global__ void __launch_bounds__(kBfsThreads) k_bfs(PW a, const uint8_t *__rest
         if (s == 0) break;
         const int per_cta = (s + C - 1) / C;
         const int segcap = 4 * per_cta;
-        if (per_cta > kBfsCtaItems || (int64_t)segcap * C > (int64_t)a.n) {
+        const long long nbase = base + (long long)C * prevcap;  // keys of the next frontier start here
+        if (per_cta > kBfsCtaItems || (int64_t)segcap * C > (int64_t)a.n ||
+            nbase + (long long)C * segcap > kKeyLimit) {
             if (me == 0 && threadIdx.x == 0) set_fallback(a, 9);  // frontier too wide: serial flood
             break;
         }
@@ -668,22 +686,14 @@ __global__ void __launch_bounds__(kBfsThreads) k_bfs(PW a, const uint8_t *__rest
         __syncthreads();
         const int pt = (cnt + kBfsThreads - 1) / kBfsThreads;
         const int j0 = threadIdx.x * pt;
-        for (int j = 0; j < pt && j0 + j < cnt; ++j) {
-            const int r = s_r[j0 + j];
-            const unsigned m = s_m[j0 + j];
-            const int key0 = (base + lo + j0 + j) * 4;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (m & (1u << k)) atomicMin(a.claim + r + off[k], key0 + k);
-                if (m & (16u << k)) atomicMin(a.inj + r + off[k], key0 + k);
-            }
-        }
-        cl.sync();
         unsigned long long win = 0;
+        seg = 0;
         for (int j = 0; j < pt && j0 + j < cnt; ++j) {
             const int r = s_r[j0 + j];
             const unsigned m = s_m[j0 + j];
-            const int key0 = (base + lo + j0 + j) * 4;
+            const int i = lo + j0 + j;  // frontier position: slot seg * prevcap + (i - offs[seg])
+            while (i >= offs[seg + 1]) ++seg;
+            const int key0 = (int)(base + (long long)seg * prevcap + (i - offs[seg])) * 4;
             int cl4[4];
             uint8_t nm4[4];
 #pragma unroll
@@ -704,24 +714,35 @@ __global__ void __launch_bounds__(kBfsThreads) k_bfs(PW a, const uint8_t *__rest
             const int b = __ffsll((long long)win) - 1;
             win &= win - 1;
             const int q = s_r[j0 + (b >> 2)] + off[b & 3];
-            Fn[me * segcap + pos] = (unsigned)q | ((unsigned long long)s_nm[j0 * 4 + b] << 32);
-            a.st[q] |= S_R;
+            const unsigned m = s_nm[j0 * 4 + b];
+            Fn[me * segcap + pos] = (unsigned)q | ((unsigned long long)m << 32);
+            const int key0 = (int)(nbase + (long long)me * segcap + pos) * 4;  // the winner's slot
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (m & (1u << k)) atomicMin(a.claim + q + off[k], key0 + k);
+                if (m & (16u << k)) atomicMin(a.inj + q + off[k], key0 + k);
+            }
             ++pos;
         }
-        if (threadIdx.x < C) *cl.map_shared_rank(&tots[me], threadIdx.x) = total;  // push the count to all
+        if (threadIdx.x < C) *cl.map_shared_rank(&tots[par ^ 1][me], threadIdx.x) = total;  // push the count to all
         unsigned long long *t = Fc;
         Fc = Fn;
         Fn = t;
         prevcap = segcap;
-        base += s;
-        ++layer;
-        cl.sync();
+        base = nbase;
     }
-    cl.sync();  // no CTA leaves while another may still read its shared counts
+    cl.sync();  // no CTA leaves while another may still push into its shared counts
     if (me == 0 && threadIdx.x == 0) {
         a.ctl[W_LAYERS] = layer;
         a.ctl[W_BFSCTAS] = C;
     }
+}
+
+// R: every pixel the BFS claimed (the seed is marked by k_state)
+__global__ void k_mark_r(PW a) {
+    if (!a.ctl[W_EVENT] || a.ctl[W_FALLBACK]) return;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x)
+        if (a.claim[p] != INT_MAX) a.st[p] |= S_R;
 }
 
 // shells: U pixels queued at T_e
@@ -1440,6 +1461,8 @@ int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int 
     NSG_COUNT_LAUNCH();
     NSG_TRY(launch_bfs(c, a, a.fgimg, s));
     NSG_LAUNCH_CHECK(c);
+    k_mark_r<<<g, kB, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     stage_mark(c, kStageWsBfs, s);
     k_shells<<<g, kB, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
