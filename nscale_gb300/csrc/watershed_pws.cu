@@ -613,7 +613,12 @@ __global__ void k_bfs_prep(PW a, uint8_t *nbm) {
 // key of the layer before (base grows by the layer's whole slot range).
 // Counts are double-buffered by layer parity, so a CTA that runs ahead into
 // the next layer never overwrites counts another CTA has yet to read.
+// While the segments stay balanced (the largest within a quarter of an equal
+// share), each CTA takes its own segment as its next chunk straight from its
+// shared memory, with no global round trip; otherwise the chunks are restaged
+// from the global frontier.  Who processes an entry never changes its key.
 constexpr int kBfsThreads = 256, kBfsCtaItems = 4096, kBfsMaxCluster = 16;
+constexpr size_t kBfsSmem = 2 * kBfsCtaItems * (sizeof(int) + 1) + 4 * kBfsCtaItems;  // dynamic shared memory
 
 __global__ void __launch_bounds__(kBfsThreads) k_bfs(PW a, const uint8_t *__restrict__ nbm) {
     namespace cg = cooperative_groups;
@@ -622,9 +627,11 @@ __global__ void __launch_bounds__(kBfsThreads) k_bfs(PW a, const uint8_t *__rest
     __shared__ int sh[40];
     __shared__ int tots[2][kBfsMaxCluster];   // entries of every CTA's segment, by layer parity
     __shared__ int offs[kBfsMaxCluster + 1];  // where each CTA's segment starts in frontier order
-    __shared__ int s_r[kBfsCtaItems];         // this CTA's chunk of the frontier
-    __shared__ uint8_t s_m[kBfsCtaItems];     // and the chunk's neighbour classes
-    __shared__ uint8_t s_nm[kBfsCtaItems * 4];  // neighbour classes of the pixels this CTA wins
+    __shared__ int s_mx;                      // the largest segment
+    extern __shared__ __align__(16) unsigned char bfs_dyn[];
+    int *s_rb = reinterpret_cast<int *>(bfs_dyn);                   // [2][kBfsCtaItems]: chunk pixels, next segment
+    uint8_t *s_mb = bfs_dyn + 2 * kBfsCtaItems * sizeof(int);         // [2][kBfsCtaItems]: their neighbour classes
+    uint8_t *s_nm = s_mb + 2 * kBfsCtaItems;                          // [kBfsCtaItems * 4]: classes of the winners
     const bool on = a.ctl[W_EVENT] && !a.ctl[W_FALLBACK];
     const int W = a.W;
     const int off[4] = {-1, 1, -W, W};
@@ -644,6 +651,11 @@ __global__ void __launch_bounds__(kBfsThreads) k_bfs(PW a, const uint8_t *__rest
     long long base = 0;  // key of slot 0 of the current frontier
     int prevcap = 1;     // slots per segment of the current frontier
     int layer = 0;
+    int cb = 0;          // which half of s_rb / s_mb holds this CTA's own segment
+    if (threadIdx.x == 0 && me == 0 && on) {
+        s_rb[0] = a.ctl[W_EP];
+        s_mb[0] = nbm[s_rb[0]];
+    }
     if (!on) {
         cl.sync();
         return;
@@ -662,32 +674,45 @@ __global__ void __launch_bounds__(kBfsThreads) k_bfs(PW a, const uint8_t *__rest
                 if (lane >= d) x += y;
             }
             if (lane <= C) offs[lane] = x - v;  // exclusive prefix; offs[C] = total
+            int mx = v;
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, d));
+            if (lane == 0) s_mx = mx;
         }
         __syncthreads();
         const int s = offs[C];
         if (s == 0) break;
         const int per_cta = (s + C - 1) / C;
-        const int segcap = 4 * per_cta;
+        const bool local = s_mx <= per_cta + per_cta / 4 + 16 && s_mx <= kBfsCtaItems;
+        const int segcap = 4 * (local ? s_mx : per_cta);
         const long long nbase = base + (long long)C * prevcap;  // keys of the next frontier start here
         if (per_cta > kBfsCtaItems || (int64_t)segcap * C > (int64_t)a.n ||
             nbase + (long long)C * segcap > kKeyLimit) {
             if (me == 0 && threadIdx.x == 0) set_fallback(a, 9);  // frontier too wide: serial flood
             break;
         }
-        const int lo = min(s, me * per_cta), hi = min(s, lo + per_cta), cnt = hi - lo;
-        // stage the chunk (the frontier is read in order: coalesced)
-        int seg = 0;
-        for (int i = lo + threadIdx.x; i < hi; i += kBfsThreads) {
-            while (i >= offs[seg + 1]) ++seg;
-            const unsigned long long e = __ldcg(Fc + seg * prevcap + (i - offs[seg]));
-            s_r[i - lo] = (int)(unsigned)e;
-            s_m[i - lo] = (uint8_t)(e >> 32);
+        int *s_r = s_rb + cb * kBfsCtaItems;
+        uint8_t *s_m = s_mb + cb * kBfsCtaItems;
+        int lo, cnt;
+        if (local) {  // this CTA's own segment, already in shared memory
+            lo = offs[me];
+            cnt = offs[me + 1] - lo;
+        } else {  // an equal chunk, staged from the global frontier (read in order: coalesced)
+            lo = min(s, me * per_cta);
+            cnt = min(s, lo + per_cta) - lo;
+            int seg = 0;
+            for (int i = lo + threadIdx.x; i < lo + cnt; i += kBfsThreads) {
+                while (i >= offs[seg + 1]) ++seg;
+                const unsigned long long e = __ldcg(Fc + seg * prevcap + (i - offs[seg]));
+                s_r[i - lo] = (int)(unsigned)e;
+                s_m[i - lo] = (uint8_t)(e >> 32);
+            }
+            __syncthreads();
         }
-        __syncthreads();
+        int seg = 0;
         const int pt = (cnt + kBfsThreads - 1) / kBfsThreads;
         const int j0 = threadIdx.x * pt;
         unsigned long long win = 0;
-        seg = 0;
         for (int j = 0; j < pt && j0 + j < cnt; ++j) {
             const int r = s_r[j0 + j];
             const unsigned m = s_m[j0 + j];
@@ -716,6 +741,10 @@ __global__ void __launch_bounds__(kBfsThreads) k_bfs(PW a, const uint8_t *__rest
             const int q = s_r[j0 + (b >> 2)] + off[b & 3];
             const unsigned m = s_nm[j0 * 4 + b];
             Fn[me * segcap + pos] = (unsigned)q | ((unsigned long long)m << 32);
+            if (pos < kBfsCtaItems) {  // this CTA's next segment, for a balanced next layer
+                s_rb[(cb ^ 1) * kBfsCtaItems + pos] = q;
+                s_mb[(cb ^ 1) * kBfsCtaItems + pos] = (uint8_t)m;
+            }
             const int key0 = (int)(nbase + (long long)me * segcap + pos) * 4;  // the winner's slot
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -730,6 +759,7 @@ __global__ void __launch_bounds__(kBfsThreads) k_bfs(PW a, const uint8_t *__rest
         Fn = t;
         prevcap = segcap;
         base = nbase;
+        cb ^= 1;
     }
     cl.sync();  // no CTA leaves while another may still push into its shared counts
     if (me == 0 && threadIdx.x == 0) {
@@ -1372,11 +1402,12 @@ int ws_flood_serial_launch(Ctx &c, const int *mk, const uint32_t *col, int *outp
 // The BFS cluster: 16 CTAs when the device can co-schedule them, else fewer.
 static int launch_bfs(Ctx &c, const PW &a, const uint8_t *nbm, cudaStream_t s) {
     NSG_CUDA_TRY(c, cudaFuncSetAttribute(k_bfs, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    NSG_CUDA_TRY(c, cudaFuncSetAttribute(k_bfs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBfsSmem));
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     cfg.blockDim = dim3(kBfsThreads);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = kBfsSmem;
     cfg.stream = s;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
