@@ -49,7 +49,7 @@ ALG_BYTES_PER_PX = 137
 # measured DRAM reads + writes per pixel of the same pipeline: ncu
 # dram__bytes_read.sum + dram__bytes_write.sum summed over every kernel of
 # one 2048 x 2048 tile run to SUCCESS (python -m nscale_gb300.tile_demo 2048)
-DRAM_BYTES_PER_PX = 401.1
+DRAM_BYTES_PER_PX = 413.6
 
 
 
