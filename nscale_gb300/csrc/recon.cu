@@ -270,6 +270,7 @@ struct Queue {
     int *stats;  // [0] tile passes, [1] row+column sweeps
     long long budget;
     int idle_limit;  // empty-queue polls before an idle CTA leaves (0: stay until done)
+    int seq_min;     // dirty lines of a 32-line group from which lanes scan one line each
 };
 
 // lane 0 only
@@ -450,7 +451,7 @@ __device__ __forceinline__ void line_scan(T (&lo)[K], T (&hi)[K], T first, T las
 // dirty lines keeps the shuffle scan (a lane-per-line pass costs the same
 // whether 1 or 32 of its lines are dirty).  uint8 only: a pixel outside the
 // image has mask 0, so min/max alone keep it 0.
-constexpr int kSeqMinLines = 8;  // dirty lines of a group from which lanes scan one line each
+constexpr int kSeqMinLines = 8;  // default: dirty lines of a group from which lanes scan one line each
 
 // Row r (tile coordinates) of the tile in `o` (pitch P, one-pixel halo), mask
 // row `m`.  chg[j] bit k: pixel j * 32 + k changed.
@@ -573,7 +574,7 @@ __device__ __forceinline__ void mark_dirty_seq(unsigned *m, const unsigned (&chg
 // write back.
 template <typename T, int TW, int TH, int P, int NW, bool HYB = false>
 __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, int cols, bool conn8, int tx, int ty,
-                                 int dirty_in, TileSmem<T, TW, TH, P> &sm) {
+                                 int dirty_in, TileSmem<T, TW, TH, P> &sm, int seq_min = kSeqMinLines) {
     static_assert(!HYB || (std::is_same<T, uint8_t>::value && NW == TH / 32 && NW == TW / 32),
                   "lane-per-line scans: uint8, one warp per 32-line group");
     constexpr int KX = TW / 32, KY = TH / 32;
@@ -649,7 +650,7 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
         for (int w = 0; w < TH / 32; ++w) {
             unsigned bits = rm[w];
             if constexpr (HYB) {
-                if (__popc(bits) >= kSeqMinLines) {
+                if (__popc(bits) >= seq_min) {
                     if (warp == w) {
                         unsigned chg[TW / 32] = {};
                         const int r = w * 32 + lane;
@@ -714,7 +715,7 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
         for (int w = 0; w < TW / 32; ++w) {
             unsigned bits = cm[w];
             if constexpr (HYB) {
-                if (__popc(bits) >= kSeqMinLines) {
+                if (__popc(bits) >= seq_min) {
                     if (warp == w) {
                         unsigned chg[TH / 32] = {};
                         if ((bits >> lane) & 1u) col_seq<TH, P>(o, sm.m, w * 32 + lane, conn8, chg);
@@ -1169,7 +1170,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) recon_cta(const T *__restrict__
             if constexpr (PACKED)
                 cta_process_tile_u8<TW, TH, NW>(mask, out, rows, cols, conn8, tx, ty, dirty, sm);
             else
-                cta_process_tile<T, TW, TH, P, NW, HYB>(mask, out, rows, cols, conn8, tx, ty, dirty, sm);
+                cta_process_tile<T, TW, TH, P, NW, HYB>(mask, out, rows, cols, conn8, tx, ty, dirty, sm, q.seq_min);
             if (threadIdx.x == 0) {
                 const unsigned edges = (unsigned)sm.edges;
                 // our top edge is the upper tile's bottom halo, and so on
@@ -1257,6 +1258,8 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
     q.dirty = dirty;
     q.idle_limit = 2048;
     if (const char *e = getenv("NSG_RECON_IDLE")) q.idle_limit = atoi(e);  // tuning knob
+    q.seq_min = kSeqMinLines;
+    if (const char *e = getenv("NSG_RECON_SEQMIN")) q.seq_min = atoi(e);  // tuning knob
     q.stats = c.ws.ctrl + C_RSTATS;
     const size_t smem = sizeof(TileOf<T, TW, TH, P, NW, PACKED>);
     auto kfn = recon_cta<T, TW, TH, P, NW, PACKED, MINB, HYB>;

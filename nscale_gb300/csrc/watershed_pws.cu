@@ -68,7 +68,7 @@ __device__ __forceinline__ int m_dir(int m) { return (m >> 9) & 3; }
 enum {
     W_FALLBACK = 0,
     W_ND,
-    W_POOL,
+    W_POOL,  // unused (kept so that the diagnostic indices stay put)
     W_E,
     W_EP,
     W_DOME,
@@ -79,6 +79,7 @@ enum {
     W_PEND,
     W_LAYERS,
     W_BFSCTAS,
+    W_DTOT,  // dummy slots reserved over all domains
 };
 
 struct PW {
@@ -89,7 +90,7 @@ struct PW {
     int *ctl;  // ctrl + C_WS
     int *status;
     // per pixel
-    uint8_t *flags, *initlvl, *pside, *st, *fgimg;
+    uint8_t *flags, *initlvl, *st, *fgimg;
     int *domroot, *dom, *lab, *utrue, *inj, *claim, *uown, *proot, *fr0, *fr1, *popl, *isroot, *rank;
     // per entry (n + pc)
     int *next, *rparent, *rlocal, *rorigin, *rmeta;
@@ -100,6 +101,9 @@ struct PW {
         *ioff, *ifill, *ilist, *cand, *pend, *pend2;
     unsigned long long *dfirst;
     int *grp;  // P3: flood group owning each pixel, -1 none (aliases the BFS frontier, free by then)
+    // per domain: dummy slots reserved (distinct U pixels beside it) and where they start;
+    // alias the root flags / root ranks, which are free once the domains are numbered
+    int *ducnt, *duoff;
 };
 
 // A pop's reads, issued together: the four neighbours' flags, markers,
@@ -168,7 +172,6 @@ __global__ void k_classify(PW a) {
         a.fgimg[p] = (f & F_FG) ? 1 : 0;
         a.lab[p] = 0;
         a.utrue[p] = -1;
-        a.pside[p] = 0;
         a.st[p] = 0;
         a.inj[p] = INT_MAX;
         a.claim[p] = INT_MAX;
@@ -197,6 +200,7 @@ __global__ void k_domain_init(PW a, const int *nd_total) {
         a.ifill[d] = 0;
         a.npop[d] = 0;
         a.cut[d] = 0;
+        a.ducnt[d] = 0;
     }
 }
 
@@ -219,6 +223,34 @@ __global__ void k_domains(PW a, const int *nd_total) {
             atomicMin(a.bby0 + d, y);
             atomicMax(a.bby1 + d, y);
         }
+    }
+}
+
+// Dummy slots: P1 pushes a U pixel (unknown, black, not queued from the
+// start) at most once per domain beside it, so each domain reserves one slot
+// per such pixel; P1 then takes slots without a global counter.
+__global__ void k_udom_count(PW a) {
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < a.n; u += gridDim.x * blockDim.x) {
+        const uint8_t f = a.flags[u];
+        if (!(f & F_UNK) || !(f & F_U) || (f & F_INIT)) continue;
+        const int nb[4] = {u - 1, u + 1, u - a.W, u + a.W};
+        int dk[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            dk[k] = a.dom[nb[k]];
+            bool seen = dk[k] < 0;
+#pragma unroll
+            for (int j = 0; j < k; ++j) seen = seen || dk[j] == dk[k];
+            if (!seen) atomicAdd(a.ducnt + dk[k], 1);
+        }
+    }
+}
+
+// the U pixel -> dummies lists (k_true_dummies walks them), from P1's slots
+__global__ void k_dummy_lists(PW a) {
+    for (int kk = blockIdx.x * blockDim.x + threadIdx.x; kk < a.pc; kk += gridDim.x * blockDim.x) {
+        const int q = a.dpix[kk];
+        if (q >= 0) a.dnextu[kk] = atomicExch(a.utrue + q, a.n + kk);
     }
 }
 
@@ -259,13 +291,25 @@ __device__ void phase1_domain(const PW &a, int d) {
         }
     int active = 0, runmax = -1, lasttop = -1, local = 0, seq = 0;
     const int base = a.doff[d];
+    int dslot = a.duoff[d];  // this domain's next dummy slot
     for (;;) {
         while (active < 256 && q.h[active] < 0) ++active;
         if (active == 256) break;
+        // the pop's reads first (the queue link, the entry and, for a pixel, its
+        // neighbourhood), so that they travel together
         int e = q.h[active];
-        q.h[active] = a.next[e];
-        if (q.h[active] < 0) q.t[active] = -1;
+        const int nx = a.next[e];
         int meta = a.rmeta[e];
+        const int p = e;
+        const int nb[4] = {p - 1, p + 1, p - W, p + W};
+        Nb4 nv;
+        uint32_t c = 0;
+        if (e < n) {
+            load_nb(a, nb, nv);
+            c = __ldg(a.col + p);
+        }
+        q.h[active] = nx;
+        if (nx < 0) q.t[active] = -1;
         int lv = m_level(meta);
         if (e >= n) {  // dummy U entry: position only
             int k = e - n;
@@ -277,11 +321,6 @@ __device__ void phase1_domain(const PW &a, int d) {
             continue;
         }
         seq++;
-        const int p = e;
-        const int nb[4] = {p - 1, p + 1, p - W, p + W};
-        Nb4 nv;
-        load_nb(a, nb, nv);
-        const uint32_t c = __ldg(a.col + p);
         int top = lv >= runmax;
         if (top) {
             runmax = lv;
@@ -317,29 +356,32 @@ __device__ void phase1_domain(const PW &a, int d) {
             if (!(fq & F_UNK)) continue;
             if (fq & F_U) {
                 if (fq & F_INIT) continue;  // queued from the start
-                // already pushed by this domain from another side?
-                int side = k ^ 1;  // side of qq on which p lies (L<->R, U<->D)
-                int ps = (int)((__ldcg((const unsigned int *)(a.pside + (qq & ~3))) >> (8 * (qq & 3))) & 15u);
+                // already pushed by this domain from another side: a pixel of d
+                // beside qq has popped with a label (the first such pixel pushed it)
                 const int nq[4] = {qq - 1, qq + 1, qq - W, qq + W};
+                int d2[4], l2q[4];
+#pragma unroll
+                for (int s2 = 0; s2 < 4; ++s2) {
+                    d2[s2] = __ldg(a.dom + nq[s2]);
+                    l2q[s2] = a.lab[nq[s2]];
+                }
                 bool mine = false;
+#pragma unroll
                 for (int s2 = 0; s2 < 4; ++s2)
-                    if ((ps >> s2) & 1)
-                        if (a.dom[nq[s2]] == d) mine = true;
+                    if (nq[s2] != p && d2[s2] == d && l2q[s2] > 0) mine = true;
                 if (mine) continue;
-                atomicOr((unsigned int *)(a.pside + (qq & ~3)), 1u << (8 * (qq & 3) + side));
-                int kk = atomicAdd(a.ctl + W_POOL, 1);
+                const int kk = dslot++;
                 if (kk >= a.pc) {
                     set_fallback(a, 4);
                     continue;
                 }
-                int id = n + kk;
+                const int id = n + kk;
+                const int l2 = cdiff(c, nv.col[k]);
                 a.dpix[kk] = qq;
                 a.ddom[kk] = d;
                 a.rparent[id] = p;
-                a.rmeta[id] = cdiff(c, nv.col[k]) | (k << 9);
+                a.rmeta[id] = l2 | (k << 9);
                 a.rlocal[id] = -1;
-                a.dnextu[kk] = atomicExch(a.utrue + qq, id);
-                int l2 = m_level(a.rmeta[id]);
                 q_push(q, a.next, l2, id);
                 if (l2 < active) active = l2;
                 continue;
@@ -958,14 +1000,16 @@ __device__ bool replay(const PW &a, int d, Q &q, int &active) {
         while (active < 256 && q.h[active] < 0) ++active;
         if (active == 256) return false;
         int e = q.h[active];
-        q.h[active] = a.next[e];
-        if (q.h[active] < 0) q.t[active] = -1;
+        const int nx = a.next[e];
         const int p = e;
         const int nb[4] = {p - 1, p + 1, p - W, p + W};
         Nb4 nv;
         load_nb(a, nb, nv);
         const uint32_t c = __ldg(a.col + p);
-        if (!(__ldg((const unsigned char *)a.flags + p) & F_FG)) return false;  // no U pop before T_e
+        const uint8_t fp = __ldg((const unsigned char *)a.flags + p);
+        q.h[active] = nx;
+        if (nx < 0) q.t[active] = -1;
+        if (!(fp & F_FG)) return false;  // no U pop before T_e
         ++local;
         int lb = 0;
 #pragma unroll
@@ -1106,8 +1150,7 @@ __device__ void phase3_group(const PW &a, int S) {
         while (active < 256 && q.h[active] < 0) ++active;
         if (active == 256) break;
         int e = q.h[active];
-        q.h[active] = a.next[e];
-        if (q.h[active] < 0) q.t[active] = -1;
+        const int nx = a.next[e];
         const int p = e;
         const int nb[4] = {p - 1, p + 1, p - W, p + W};
         Nb4 nv;
@@ -1120,6 +1163,8 @@ __device__ void phase3_group(const PW &a, int S) {
             gq[k] = __ldg(a.grp + nb[k]);
         }
         const uint32_t c = __ldg(a.col + p);
+        q.h[active] = nx;
+        if (nx < 0) q.t[active] = -1;
         int lb = 0;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -1319,7 +1364,6 @@ void carve(PW &a, char *base, size_t *used_out) {
     Carve cv{base};
     a.flags = cv.take<uint8_t>(n);
     a.initlvl = cv.take<uint8_t>(n);
-    a.pside = cv.take<uint8_t>(n + 4);
     a.st = cv.take<uint8_t>(n);
     a.fgimg = cv.take<uint8_t>(n);
     a.domroot = cv.take<int>(n);
@@ -1336,6 +1380,8 @@ void carve(PW &a, char *base, size_t *used_out) {
     a.popl = cv.take<int>(n);
     a.isroot = cv.take<int>(n);
     a.rank = cv.take<int>(n);
+    a.ducnt = a.isroot;  // the root flags are scanned into ranks before the domains are initialised
+    a.duoff = a.rank;    // the ranks are read by k_domains only
     a.next = cv.take<int>(np);
     a.rparent = cv.take<int>(np);
     a.rlocal = cv.take<int>(np);
@@ -1467,14 +1513,22 @@ int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int 
     k_domains<<<g, kB, 0, s>>>(a, a.ctl + W_ND);
     NSG_COUNT_LAUNCH();
     NSG_TRY(exclusive_scan_i32(c, a.dsize, a.doff, n, nullptr, s, a.ctl + W_ND));  // per-domain: nd entries
+    k_udom_count<<<g, kB, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
+    NSG_TRY(exclusive_scan_i32(c, a.ducnt, a.duoff, n, a.ctl + W_DTOT, s, a.ctl + W_ND));
+    NSG_CUDA_TRY(c, cudaMemsetAsync(a.dpix, 0xff, sizeof(int) * (size_t)a.pc, s));  // -1: slot unused
     NSG_LAUNCH_CHECK(c);
-    // P1: one thread per domain (the grid covers the largest possible count)
-    const int gd = c.sm_count * 32;  // per-domain kernels: grid-stride over the domain count
+    // P1: one thread per domain
+    // per-domain kernels: grid-stride over the domain count (on the device); 64-thread
+    // blocks, 4 per SM cover 38,912 domains at once (a 4096^2 tile has a few thousand)
+    const int gd = c.sm_count * 4;
     k_phase1<<<gd, 64, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     stage_mark(c, kStageWsP1, s);
     // P2
+    k_dummy_lists<<<g, kB, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
     k_true_dummies<<<g, kB, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
     k_candidates<<<g, kB, 0, s>>>(a);
