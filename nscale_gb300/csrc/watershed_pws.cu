@@ -255,8 +255,11 @@ __global__ void k_dummy_lists(PW a) {
 }
 
 // ---------------------------------------------------------------- queues ----
+// 256 FIFO queues (one per level) as heads and tails of lists linked
+// through `next`; the heads and tails live wherever the caller puts them
+// (P1: shared memory, P3: local memory)
 struct Q {
-    int h[256], t[256];
+    int *h, *t;
 };
 __device__ __forceinline__ void q_init(Q &q) {
     for (int i = 0; i < 256; ++i) q.h[i] = q.t[i] = -1;
@@ -268,15 +271,24 @@ __device__ __forceinline__ void q_push(Q &q, int *next, int lvl, int e) {
     q.t[lvl] = e;
 }
 
-// P1: flood domain d to completion, U pixels are dummies.
-__device__ void phase1_domain(const PW &a, int d);
-__global__ void __launch_bounds__(64) k_phase1(PW a) {
+// P1: flood domain d to completion, U pixels are dummies.  One warp per
+// block; each thread keeps its queue heads and tails in shared memory (a
+// row of kQPitch ints, odd, so that threads at the same level hit different
+// banks): every pop and push touches them, and thread-private local memory
+// would share the L1 with the flood's global reads.
+constexpr int kP1Threads = 32, kQPitch = 513;
+constexpr size_t kP1Smem = sizeof(int) * kP1Threads * kQPitch;
+__device__ void phase1_domain(const PW &a, int d, Q &q);
+__global__ void __launch_bounds__(kP1Threads) k_phase1(PW a) {
+    extern __shared__ int qsm[];
     const int nd = a.ctl[W_ND];
-    for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < nd; d += gridDim.x * blockDim.x) phase1_domain(a, d);
+    Q q;
+    q.h = qsm + threadIdx.x * kQPitch;
+    q.t = q.h + 256;
+    for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < nd; d += gridDim.x * blockDim.x) phase1_domain(a, d, q);
 }
 
-__device__ void phase1_domain(const PW &a, int d) {
-    Q q;
+__device__ void phase1_domain(const PW &a, int d, Q &q) {
     q_init(q);
     const int W = a.W, n = a.n;
     for (int y = a.bby0[d]; y <= a.bby1[d]; ++y)
@@ -1055,19 +1067,24 @@ __device__ bool replay(const PW &a, int d, Q &q, int &active) {
     return true;
 }
 
-__device__ void phase3_group(const PW &a, int S);
-__global__ void __launch_bounds__(64) k_phase3(PW a) {
+// P3: one thread per flood group, the group's queue in shared memory as in
+// P1 (the members' queues of a multi-member merge stay in local memory)
+__device__ void phase3_group(const PW &a, int S, Q &q);
+__global__ void __launch_bounds__(kP1Threads) k_phase3(PW a) {
+    extern __shared__ int qsm[];
     const int nd = a.ctl[W_ND];
     if (a.ctl[W_FALLBACK] || !a.ctl[W_EVENT]) return;
+    Q q;
+    q.h = qsm + threadIdx.x * kQPitch;
+    q.t = q.h + 256;
     for (int S = blockIdx.x * blockDim.x + threadIdx.x; S < nd; S += gridDim.x * blockDim.x)
-        if (a.mcount[S] > 0) phase3_group(a, S);
+        if (a.mcount[S] > 0) phase3_group(a, S, q);
 }
-__device__ void phase3_group(const PW &a, int S) {
+__device__ void phase3_group(const PW &a, int S, Q &q) {
     const int nm = a.mcount[S];
     const int *mem = a.mlist + a.moff[S];
     const int X = a.ctl[W_X];
     const int W = a.W;
-    Q q;
     q_init(q);
     int active = 0;
     if (nm == 1) {
@@ -1087,7 +1104,8 @@ __device__ void phase3_group(const PW &a, int S) {
         int *pend = a.pend + pb, *tmp = a.pend2 + pb;
         int np = 0;
         for (int m = 0; m < nm; ++m) {
-            Q qm;
+            int qmh[256], qmt[256];
+            Q qm{qmh, qmt};
             q_init(qm);
             int act = 0;
             if (!replay(a, mem[m], qm, act)) {
@@ -1522,7 +1540,8 @@ int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int 
     // per-domain kernels: grid-stride over the domain count (on the device); 64-thread
     // blocks, 4 per SM cover 38,912 domains at once (a 4096^2 tile has a few thousand)
     const int gd = c.sm_count * 4;
-    k_phase1<<<gd, 64, 0, s>>>(a);
+    NSG_CUDA_TRY(c, cudaFuncSetAttribute(k_phase1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kP1Smem));
+    k_phase1<<<gd * 64 / kP1Threads, kP1Threads, kP1Smem, s>>>(a);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     stage_mark(c, kStageWsP1, s);
@@ -1578,7 +1597,8 @@ int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int 
     k_pixel_groups<<<g, kB, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
-    k_phase3<<<gd, 64, 0, s>>>(a);
+    NSG_CUDA_TRY(c, cudaFuncSetAttribute(k_phase3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kP1Smem));
+    k_phase3<<<gd * 64 / kP1Threads, kP1Threads, kP1Smem, s>>>(a);
     NSG_COUNT_LAUNCH();
     stage_mark(c, kStageWsP3, s);
     k_assemble<<<g, kB, 0, s>>>(a);
