@@ -61,7 +61,6 @@ constexpr uint8_t F_UNK = 1, F_U = 2, F_INIT = 4, F_FG = 8, F_BORDER = 16;
 constexpr uint8_t S_POPPED = 1, S_QUEUED = 2, S_R = 4, S_CERTAIN = 8, S_ACTIVE = 16, S_POCKET = 32;
 // rec_meta: level (8) | top << 8 | dir << 9
 __device__ __forceinline__ int m_level(int m) { return m & 255; }
-__device__ __forceinline__ int m_top(int m) { return (m >> 8) & 1; }
 __device__ __forceinline__ int m_dir(int m) { return (m >> 9) & 3; }
 
 // control block indices (ctrl + C_WS)

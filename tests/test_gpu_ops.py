@@ -75,6 +75,25 @@ def test_imreconstruct_u8(cuda, orc, shape, conn):
                                   orc.imreconstruct(marker, mask, conn))
 
 
+# every launch form of the uint8 reconstruction (tuning knobs, read at each
+# call): lane-per-line scans at several thresholds, shuffle scans at each warp
+# count and register budget, the packed strip pass; one result for all
+@pytest.mark.parametrize("knobs", [
+    {"NSG_RECON_SEQMIN": "1"}, {"NSG_RECON_SEQMIN": "33"}, {"NSG_RECON_CTAS_PER_SM": "1"},
+    {"NSG_RECON_HYB": "0"}, {"NSG_RECON_HYB": "0", "NSG_RECON_MINB": "2"}, {"NSG_RECON_WARPS": "16"},
+    {"NSG_RECON_WARPS": "32"}, {"NSG_RECON_PACKED": "1", "NSG_RECON_HYB": "0"}, {"NSG_RECON_MAX_CTAS": "3"},
+])
+@pytest.mark.parametrize("conn", [4, 8])
+def test_imreconstruct_u8_launch_forms(cuda, orc, conn, knobs, monkeypatch):
+    from nscale_gb300 import morphologic_operations as MO
+    from nscale_gb300 import synth
+    for k, v in knobs.items():
+        monkeypatch.setenv(k, v)
+    marker, mask = synth.recon_inputs(700, 901, seed=0x5EED0021 + conn)
+    np.testing.assert_array_equal(N(MO.imreconstruct(T(marker), T(mask), conn)),
+                                  orc.imreconstruct(marker, mask, conn))
+
+
 @pytest.mark.parametrize("shape", [(1, 1), (37, 1), (64, 64), (97, 131), (600, 700)])
 @pytest.mark.parametrize("conn", [4, 8])
 def test_imreconstruct_f32(cuda, orc, shape, conn):
