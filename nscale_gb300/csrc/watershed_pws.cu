@@ -969,6 +969,38 @@ __global__ void k_inj_count(PW a, int pass) {
         else a.ilist[a.ioff[r] + atomicAdd(a.ifill + r, 1)] = p;
     }
 }
+// A group of one domain starts P3 from the domain's state at T_e, read from
+// P1's records instead of replaying its flood: popped pixels keep their P1
+// labels, pixels queued at T_e are IN_QUEUE, the rest 0; an active shell the
+// domain owns becomes a real entry with its true dummy's pusher and level.
+// (A shell whose dummy popped before the domain's cut is a U pop before T_e:
+// the exactness condition the replay checks, so the serial flood takes over.)
+__global__ void k_p3_state(PW a) {
+    if (!a.ctl[W_EVENT] || a.ctl[W_FALLBACK]) return;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
+        const uint8_t f = a.flags[p];
+        if (f & F_FG) {
+            if (a.mcount[a.sup[a.dom[p]]] != 1) continue;  // several members: P3 replays them
+            const uint8_t s = a.st[p];
+            if (s & S_POPPED) continue;
+            a.lab[p] = (s & S_QUEUED) ? IN_QUEUE : 0;
+        } else if (f & F_U) {
+            if (!(a.st[p] & S_ACTIVE)) continue;
+            const int te = a.utrue[p];
+            if (te < a.n) continue;
+            const int d = a.ddom[te - a.n];
+            if (a.mcount[a.sup[d]] != 1) continue;
+            if (a.rlocal[te] < a.cut[d]) {
+                set_fallback(a, 11);
+                continue;
+            }
+            a.lab[p] = IN_QUEUE;
+            a.rparent[p] = a.rparent[te];
+            a.rmeta[p] = a.rmeta[te] & ~(1 << 8);
+        }
+    }
+}
+
 // the flood group owning each pixel (the owned() test of P3, precomputed)
 __global__ void k_pixel_groups(PW a) {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
@@ -1066,6 +1098,48 @@ __device__ bool replay(const PW &a, int d, Q &q, int &active) {
     return true;
 }
 
+// The queue of domain d at T_e, from P1's records: the entries queued at T_e
+// in the order the flood pushed them — first the initial ones (raster order),
+// then, pop by pop up to the cut, the neighbours each pop pushed (direction
+// order).  The reads of one pop do not depend on the previous pop's, so the
+// walk streams instead of replaying the flood's dependent chain.
+__device__ void queue_at_te(const PW &a, int d, Q &q) {
+    const int W = a.W, n = a.n;
+    for (int y = a.bby0[d]; y <= a.bby1[d]; ++y)
+        for (int x = a.bbx0[d]; x <= a.bbx1[d]; ++x) {
+            const int p = y * W + x;
+            if (__ldg(a.dom + p) != d) continue;
+            if ((__ldg((const unsigned char *)a.flags + p) & F_INIT) &&
+                (__ldg((const unsigned char *)a.st + p) & S_QUEUED))
+                q_push(q, a.next, __ldg((const unsigned char *)a.initlvl + p), p);
+        }
+    const int base = a.doff[d], cutd = a.cut[d];
+#pragma unroll 2
+    for (int i = 0; i < cutd; ++i) {
+        const int p = __ldg(a.popl + base + i);
+        const int nb[4] = {p - 1, p + 1, p - W, p + W};
+        uint8_t f[4], sq[4];
+        int par[4], te[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            f[k] = __ldg((const unsigned char *)a.flags + nb[k]);
+            sq[k] = __ldg((const unsigned char *)a.st + nb[k]);
+            par[k] = __ldg(a.rparent + nb[k]);
+            te[k] = __ldg(a.utrue + nb[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int qq = nb[k];
+            if (f[k] & F_FG) {
+                if ((sq[k] & S_QUEUED) && par[k] == p) q_push(q, a.next, m_level(__ldg(a.rmeta + qq)), qq);
+            } else if ((f[k] & F_U) && (sq[k] & S_ACTIVE) && te[k] >= n) {
+                if (__ldg(a.ddom + te[k] - n) == d && __ldg(a.rparent + te[k]) == p)
+                    q_push(q, a.next, m_level(__ldg(a.rmeta + te[k])), qq);
+            }
+        }
+    }
+}
+
 // P3: one thread per flood group, the group's queue in shared memory as in
 // P1 (the members' queues of a multi-member merge stay in local memory)
 __device__ void phase3_group(const PW &a, int S, Q &q);
@@ -1087,10 +1161,8 @@ __device__ void phase3_group(const PW &a, int S, Q &q) {
     q_init(q);
     int active = 0;
     if (nm == 1) {
-        if (!replay(a, mem[0], q, active)) {
-            set_fallback(a, 11);
-            return;
-        }
+        queue_at_te(a, mem[0], q);  // labels and shells were set by k_p3_state
+        active = 0;
     } else {
         // replay every member, collect pending entries, merge them by push time
         int total = 0;
@@ -1594,6 +1666,8 @@ int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int 
     k_reset_owned_u<<<g, kB, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
     k_pixel_groups<<<g, kB, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
+    k_p3_state<<<g, kB, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     NSG_CUDA_TRY(c, cudaFuncSetAttribute(k_phase3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kP1Smem));
