@@ -30,13 +30,14 @@
 //       the first U pixel e floods, at level 0, every black unknown pixel
 //       connected to it (region R) in FIFO BFS order; fg pixels that R touches
 //       are queued with R's label at their colour level, in that BFS order —
-//       a single-CTA, rank-ordered layer-synchronous BFS computes the exact
+//       a layer-synchronous BFS in one thread-block cluster computes the exact
 //       order.  U pixels queued before T_e ("shells") and black regions R does
 //       not reach ("pockets") are attached to the domains they touch; domains
 //       that share a shell or a pocket are merged into one flood group.
-//   P3  one thread per group replays each member to its T_e state, merges the
-//       members' pending queues by push time, appends R's pushes and floods the
-//       group to completion.
+//   P3  one thread per group brings each member to its T_e state (a group of
+//       one domain from P1's records, a larger group by replaying its members),
+//       merges the members' pending queues by push time, appends R's pushes and
+//       floods the group to completion.
 // Whenever an exactness condition fails (the first U pop at level 0, a
 // watershed-labelled first U pixel, an unowned active shell, an overflow) a
 // device flag makes the serial flood (ws_flood_serial) produce the result.
