@@ -12,11 +12,13 @@
 //    owns a tile at a time and keeps it, a one-pixel halo and its mask in
 //    shared memory;
 //  * inside the tile, row phases and column phases alternate.  In a row
-//    phase each warp takes whole rows: the cross-row step (the neighbours in
-//    the rows above and below) is elementwise, and the along-row dependence
+//    phase the cross-row step (the neighbours in the rows above and below) is
+//    elementwise, and the along-row dependence
 //    out[x] = clamp(out[x-1], lo[x], hi[x]) of the raster and anti-raster
-//    scans is a composition of clamp functions, evaluated as a prefix scan
-//    with warp shuffles; column phases do the same down and up the columns;
+//    scans is either run pixel by pixel with one lane per row (uint8, when
+//    many rows of a 32-row group are dirty) or evaluated by a whole warp per
+//    row as a prefix composition of clamp functions with warp shuffles;
+//    column phases do the same down and up the columns;
 //  * only dirty lines are scanned: a pixel changed by a row phase dirties its
 //    column and the two next to it for the following column phase, and the
 //    other way round, so a pass costs what actually propagates;
