@@ -70,3 +70,30 @@ def test_pool_and_server_host_checks(nsg):
     assert nsg.nsg_pool_set_tuning(None, C.byref(t)) == _lib.ERR_ARG
     assert nsg.nsg_pool_set_timing(None, 1) == _lib.ERR_ARG
     assert nsg.nsg_pool_stage_times(None, None, 0, None) == _lib.ERR_ARG
+
+
+def test_package_import_sets_hardware_queue_default():
+    """Importing the package before CUDA starts asks for 32 hardware work
+    queues (one per tile stream of the batched form); a caller's value wins."""
+    import sys
+    code = ("import os; os.environ.pop('CUDA_DEVICE_MAX_CONNECTIONS', None); import nscale_gb300; "
+            "print(os.environ['CUDA_DEVICE_MAX_CONNECTIONS'])")
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=ROOT)
+    assert out.stdout.strip() == "32", out.stderr
+    env = dict(os.environ, CUDA_DEVICE_MAX_CONNECTIONS="4")
+    code = "import os, nscale_gb300; print(os.environ['CUDA_DEVICE_MAX_CONNECTIONS'])"
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=ROOT, env=env)
+    assert out.stdout.strip() == "4", out.stderr
+
+
+def test_autotune_worker_cap_follows_free_memory(nsg, monkeypatch):
+    """max_workers: contexts that fit in the free device memory after a reserve
+    (a quarter of it, at least 8 GiB), never fewer than one."""
+    import torch
+    from nscale_gb300 import _lib, autotune
+    per = _lib.load().nsg_pool_context_bytes(4096, 4096)
+    assert per > 0
+    for free, want in [(280 << 30, int((280 * 0.75 * (1 << 30)) // per)), (16 << 30, int((8 << 30) // per)),
+                       (1 << 30, 1)]:
+        monkeypatch.setattr(torch.cuda, "mem_get_info", lambda device=0, f=free: (f, 288 << 30))
+        assert autotune.max_workers(4096, 4096, 0) == max(1, want)
