@@ -75,6 +75,20 @@ def test_imreconstruct_u8(cuda, orc, shape, conn):
                                   orc.imreconstruct(marker, mask, conn))
 
 
+@pytest.mark.parametrize("shape", [(300, 517), (1024, 777)])
+@pytest.mark.parametrize("conn", [4, 8])
+def test_imreconstruct_u8_rough(cuda, orc, shape, conn):
+    """Per-pixel random mask and sparse seeds: propagation follows single-pixel
+    (often diagonal) paths across many tiles, the case that exercises the
+    dirty-line and neighbour-notification rules (smooth masks rarely do)."""
+    from nscale_gb300 import morphologic_operations as MO
+    g = np.random.default_rng(0x5EED0041 + shape[0] + conn)
+    mask = g.integers(0, 256, size=shape).astype(np.uint8)
+    marker = np.where(g.random(shape) < 0.01, mask, 0).astype(np.uint8)
+    np.testing.assert_array_equal(N(MO.imreconstruct(T(marker), T(mask), conn)),
+                                  orc.imreconstruct(marker, mask, conn))
+
+
 # every launch form of the uint8 reconstruction (tuning knobs, read at each
 # call): lane-per-line scans at several thresholds, shuffle scans at each warp
 # count and register budget, the packed strip pass; one result for all
