@@ -162,6 +162,10 @@ def test_push_dedupe_and_queue_at_te(seed):
     rec, _ = flood(kind, mk, col, init, W, "neighbours")
     assert rec["pops"] == rec_sides["pops"]
     assert [d[:4] for d in rec["dummies"]] == [d[:4] for d in rec_sides["dummies"]]
+    # k_udom_count's reservation holds: one dummy slot per distinct U pixel beside the domain
+    beside = {p + o for p in fg for o in (-1, 1, -W, W) if kind[p + o] == "U"}
+    assert len(rec["dummies"]) <= len(beside)
+    assert len({d[0] for d in rec["dummies"]}) == len(rec["dummies"])
     # P3's start, for every cut and a random set of active shells owned by the domain
     shells = {d[0] for d in rec["dummies"] if rng.random() < 0.6}
     for cut in range(len(rec["pops"]) + 1):
