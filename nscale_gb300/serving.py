@@ -40,7 +40,9 @@ def _bbox_array(L, ptr, n: int) -> np.ndarray:
 
 class TilePool:
     """`workers` tiles in flight on `device`, each worker a context sized for
-    max_rows x max_cols (nsg_pool_create)."""
+    max_rows x max_cols (nsg_pool_create).  32 workers is the measured best for
+    4096 x 4096 tiles on GB300 (4 GiB of device memory each);
+    `nscale_gb300.autotune` picks the count and launch shapes for a batch."""
 
     def __init__(self, max_rows: int, max_cols: int, workers: int = 8, device: int = 0):
         self.L = _lib.load()
