@@ -73,8 +73,11 @@ int nsg_context_create(nsg_context **ctx, int max_rows, int max_cols, int device
 int nsg_context_destroy(nsg_context *ctx);
 const char *nsg_context_last_error(const nsg_context *ctx);
 size_t nsg_context_bytes(const nsg_context *ctx);
-/* Device-wait budget for persistent kernels (iterations); tests set it low to
- * exercise NSG_ERR_TIMEOUT.  0 restores the default. */
+/* Device-wait budget (iterations) of every bounded device loop: the
+ * persistent kernels' queue waits and the union-find's find steps and hooking
+ * retries (per union).  A loop that runs out sets the device status word and
+ * the call returns NSG_ERR_TIMEOUT; tests set it low to exercise that.  0
+ * restores the default (2^26). */
 int nsg_context_set_spin_budget(nsg_context *ctx, long long iterations);
 /* Launch-shape tuning (no counterpart in the reference, whose kernels have
  * fixed shapes): results do not depend on it.  recon_max_ctas caps the
@@ -134,10 +137,14 @@ int nsg_imfill_holes_u8(nsg_context *ctx, const uint8_t *img, uint8_t *out, int 
  *    pointers, sizes or connectivity return NSG_ERR_ARG.
  *  - The first call on each device looks up the array's device address (with
  *    that device current); make that first call before any stream capture.
- *  - The call only enqueues work on `stream` and returns; `out` is ready when
- *    the stream reaches it.  All calls share the one array, so calls whose
- *    work overlaps on the GPU (other streams, other host threads) race:
- *    order them on one stream or synchronise between them. */
+ *  - The call enqueues its work on `stream`, then reads its device status
+ *    word back into host stack memory and waits for the stream, so `out` is
+ *    complete on return.  NSG_ERR_TIMEOUT means the union-find ran out of
+ *    its step budget (NSG_SPIN_BUDGET in the environment, read at each call;
+ *    default 2^26) and `out` must not be used.
+ *  - All calls share the one array, so calls whose work overlaps on the GPU
+ *    (other streams, other host threads) race: order them on one stream or
+ *    synchronise between them. */
 #define NSG_NOALLOC_MAX_PIXELS (4194304) /* e.g. 2048 x 2048 */
 int nsg_imfill_holes_u8_noalloc(const uint8_t *img, uint8_t *out, int rows, int cols, int conn,
                                 nsg_stream_t stream);

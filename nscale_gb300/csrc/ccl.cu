@@ -22,6 +22,7 @@
 // bwselect and imfillHoles are all "label the mask, flag the components that
 // touch a seed (or the image border), select".
 #include <limits.h>
+#include <stdlib.h>
 
 #include <mutex>
 
@@ -33,21 +34,36 @@ namespace {
 
 constexpr int kB = 256;
 
-__device__ __forceinline__ int find_root(int *parent, int x) {
+// Bounded union: every find step and every lost hooking race counts against
+// `budget`; when it runs out the union is abandoned, DEV_TIMEOUT is set in
+// the device status word and the host call returns NSG_ERR_TIMEOUT (the
+// labels are then incomplete, never silently returned as correct).
+struct UfGuard {
+    long long budget;
+    int *status;
+};
+
+__device__ __forceinline__ int find_root_counted(int *parent, int x, long long &steps) {
     for (;;) {
         int p = __ldcg(parent + x);
         if (p == x) return x;
         int gp = __ldcg(parent + p);
         if (gp != p) parent[x] = gp;  // path halving (benign race: ancestors only)
         x = p;
+        ++steps;
     }
 }
 
-__device__ __forceinline__ void unite(int *parent, int a, int b) {
-    for (int guard = 0; guard < 1 << 24; ++guard) {
-        a = find_root(parent, a);
-        b = find_root(parent, b);
+__device__ __forceinline__ void unite(int *parent, int a, int b, const UfGuard &g) {
+    long long steps = 0;
+    for (;;) {
+        a = find_root_counted(parent, a, steps);
+        b = find_root_counted(parent, b, steps);
         if (a == b) return;
+        if (steps >= g.budget) {
+            atomicOr(g.status, DEV_TIMEOUT);
+            return;
+        }
         if (a < b) {
             int t = a;
             a = b;
@@ -56,42 +72,7 @@ __device__ __forceinline__ void unite(int *parent, int a, int b) {
         int old = atomicMin(parent + a, b);
         if (old == a) return;
         a = old;
-    }
-}
-
-template <int MODE>
-__device__ __forceinline__ bool fg(uint8_t v) {
-    return MODE == CCL_NOT255 ? v != 255 : v != 0;
-}
-template <int MODE>
-__device__ __forceinline__ bool joins(uint8_t a, uint8_t b) {
-    if (MODE == CCL_EQUAL) return a == b && a != 0;
-    if (MODE == CCL_NONZERO) return a != 0 && b != 0;
-    return a != 255 && b != 255;
-}
-
-template <int MODE>
-__global__ void ccl_init(const uint8_t *__restrict__ img, int *__restrict__ parent, int64_t n) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        parent[i] = fg<MODE>(img[i]) ? (int)i : -1;
-}
-
-template <int MODE>
-__global__ void ccl_merge(const uint8_t *__restrict__ img, int *parent, int rows, int cols, int conn) {
-    int64_t n = (int64_t)rows * cols;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        uint8_t p = img[i];
-        if (!fg<MODE>(p)) continue;
-        int y = (int)(i / cols), x = (int)(i - (int64_t)y * cols);
-        if (x > 0 && joins<MODE>(p, img[i - 1])) unite(parent, (int)i, (int)(i - 1));
-        if (y > 0) {
-            int64_t u = i - cols;
-            if (joins<MODE>(p, img[u])) unite(parent, (int)i, (int)u);
-            if (conn == 8) {
-                if (x > 0 && joins<MODE>(p, img[u - 1])) unite(parent, (int)i, (int)(u - 1));
-                if (x < cols - 1 && joins<MODE>(p, img[u + 1])) unite(parent, (int)i, (int)(u + 1));
-            }
-        }
+        ++steps;
     }
 }
 
@@ -225,45 +206,21 @@ __global__ void __launch_bounds__(256) ccl_local(Pred pr, int *__restrict__ pare
 // unions of neighbour pairs that cross a tile border (backward neighbours:
 // left, up, up-left, up-right, the pairs ConnComponents::label visits)
 template <typename Pred>
-__global__ void ccl_border(Pred pr, int *parent, int rows, int cols, int conn) {
+__global__ void ccl_border(Pred pr, int *parent, int rows, int cols, int conn, UfGuard ug) {
     int64_t n = (int64_t)rows * cols;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int y = (int)(i / cols), x = (int)(i - (int64_t)y * cols);
         int bx = x & (LT - 1), by = y & (LT - 1);
         if (bx != 0 && by != 0 && bx != LT - 1) continue;
         if (!pr.fg(i)) continue;
-        if (x > 0 && bx == 0 && pr.joins(i, i - 1)) unite(parent, (int)i, (int)(i - 1));
+        if (x > 0 && bx == 0 && pr.joins(i, i - 1)) unite(parent, (int)i, (int)(i - 1), ug);
         if (y > 0) {
             int64_t u = i - cols;
-            if (by == 0 && pr.joins(i, u)) unite(parent, (int)i, (int)u);
+            if (by == 0 && pr.joins(i, u)) unite(parent, (int)i, (int)u, ug);
             if (conn == 8) {
-                if (x > 0 && (bx == 0 || by == 0) && pr.joins(i, u - 1)) unite(parent, (int)i, (int)(u - 1));
+                if (x > 0 && (bx == 0 || by == 0) && pr.joins(i, u - 1)) unite(parent, (int)i, (int)(u - 1), ug);
                 if (x < cols - 1 && (bx == LT - 1 || by == 0) && pr.joins(i, u + 1))
-                    unite(parent, (int)i, (int)(u + 1));
-            }
-        }
-    }
-}
-
-// float plateaus among valid pixels (local extrema floods)
-__global__ void cclf_init(const uint8_t *__restrict__ valid, int *__restrict__ parent, int64_t n) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        parent[i] = valid[i] ? (int)i : -1;
-}
-__global__ void cclf_merge(const float *__restrict__ val, const uint8_t *__restrict__ valid, int *parent, int rows,
-                           int cols, int conn) {
-    int64_t n = (int64_t)rows * cols;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        if (!valid[i]) continue;
-        float p = val[i];
-        int y = (int)(i / cols), x = (int)(i - (int64_t)y * cols);
-        if (x > 0 && valid[i - 1] && val[i - 1] == p) unite(parent, (int)i, (int)(i - 1));
-        if (y > 0) {
-            int64_t u = i - cols;
-            if (valid[u] && val[u] == p) unite(parent, (int)i, (int)u);
-            if (conn == 8) {
-                if (x > 0 && valid[u - 1] && val[u - 1] == p) unite(parent, (int)i, (int)(u - 1));
-                if (x < cols - 1 && valid[u + 1] && val[u + 1] == p) unite(parent, (int)i, (int)(u + 1));
+                    unite(parent, (int)i, (int)(u + 1), ug);
             }
         }
     }
@@ -503,7 +460,8 @@ int ccl_u8(Ctx &c, const uint8_t *img, int32_t *parent, int rows, int cols, int 
     dim3 grid((cols + LT - 1) / LT, (rows + LT - 1) / LT);
     ccl_local<PredU8><<<grid, 256, 0, s>>>(pr, parent, rows, cols, conn);
     NSG_COUNT_LAUNCH();
-    ccl_border<PredU8><<<blocks(c, n), kB, 0, s>>>(pr, parent, rows, cols, conn);
+    ccl_border<PredU8><<<blocks(c, n), kB, 0, s>>>(pr, parent, rows, cols, conn,
+                                                   UfGuard{c.spin_budget, c.ws.ctrl + C_STATUS});
     NSG_COUNT_LAUNCH();
     if (zero_flags)
         ccl_flatten_zero<<<blocks(c, n), kB, 0, s>>>(parent, n, zero_flags);
@@ -521,7 +479,8 @@ int ccl_f32_masked(Ctx &c, const float *val, const uint8_t *valid, int32_t *pare
     dim3 grid((cols + LT - 1) / LT, (rows + LT - 1) / LT);
     ccl_local<PredF32><<<grid, 256, 0, s>>>(pr, parent, rows, cols, conn);
     NSG_COUNT_LAUNCH();
-    ccl_border<PredF32><<<blocks(c, n), kB, 0, s>>>(pr, parent, rows, cols, conn);
+    ccl_border<PredF32><<<blocks(c, n), kB, 0, s>>>(pr, parent, rows, cols, conn,
+                                                    UfGuard{c.spin_budget, c.ws.ctrl + C_STATUS});
     NSG_COUNT_LAUNCH();
     ccl_flatten<<<blocks(c, n), kB, 0, s>>>(parent, n);
     NSG_COUNT_LAUNCH();
@@ -621,13 +580,17 @@ int bbox_dev(Ctx &c, const int32_t *labels, int rows, int cols, int32_t *d_bbox,
 // work planes (component labels and per-component border flags) from one
 // file-scope device array instead of the context arena.  The array is part
 // of this library's device image: every GPU that loads the library holds it
-// (NSG_NOALLOC_MAX_PIXELS * 8 bytes) until the process exits.
+// (NSG_NOALLOC_MAX_PIXELS * 8 bytes) until the process exits.  A second
+// file-scope word is the call's device status word: the union-find's bounded
+// retries report through it, and the call reads it back before returning.
 namespace {
 
 __device__ __align__(256) int g_noalloc_scratch[2 * (int64_t)NSG_NOALLOC_MAX_PIXELS];
+__device__ int g_noalloc_status;
 
 struct NoAllocScratch {
-    int *base = nullptr;  // device address of g_noalloc_scratch on this device
+    int *base = nullptr;    // device address of g_noalloc_scratch on this device
+    int *status = nullptr;  // device address of g_noalloc_status on this device
     int sm_count = 0;
 };
 constexpr int kNoAllocDevices = 64;
@@ -651,16 +614,34 @@ int noalloc_scratch(NoAllocScratch *out) {
             cudaGetLastError();
             return NSG_ERR_CUDA;
         }
+        void *ps = nullptr;
+        if (cudaGetSymbolAddress(&ps, g_noalloc_status) != cudaSuccess || !ps) {
+            cudaGetLastError();
+            return NSG_ERR_CUDA;
+        }
         int sms = 0;
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
             cudaGetLastError();
             return NSG_ERR_CUDA;
         }
         e.sm_count = sms;
+        e.status = static_cast<int *>(ps);
         e.base = static_cast<int *>(p);
     }
     *out = e;
     return NSG_SUCCESS;
+}
+
+// union-find step budget of the no-allocation entry (it has no context to
+// carry one): NSG_SPIN_BUDGET in the environment, read at each call, else
+// the context default
+long long noalloc_spin_budget() {
+    const char *e = getenv("NSG_SPIN_BUDGET");
+    if (e) {
+        const long long v = atoll(e);
+        if (v > 0) return v;
+    }
+    return 1ll << 26;
 }
 
 int noalloc_blocks(int sm_count, int64_t n) {
@@ -690,9 +671,13 @@ extern "C" int nsg_imfill_holes_u8_noalloc(const uint8_t *img, uint8_t *out, int
     PredU8 pr{img, CCL_NOT255};
     const int g = noalloc_blocks(sc.sm_count, n);
     dim3 grid((cols + LT - 1) / LT, (rows + LT - 1) / LT);
+    if (cudaMemsetAsync(sc.status, 0, sizeof(int), s) != cudaSuccess) {
+        cudaGetLastError();
+        return NSG_ERR_CUDA;
+    }
     ccl_local<PredU8><<<grid, 256, 0, s>>>(pr, lab, rows, cols, conn);
     NSG_COUNT_LAUNCH();
-    ccl_border<PredU8><<<g, kB, 0, s>>>(pr, lab, rows, cols, conn);
+    ccl_border<PredU8><<<g, kB, 0, s>>>(pr, lab, rows, cols, conn, UfGuard{noalloc_spin_budget(), sc.status});
     NSG_COUNT_LAUNCH();
     ccl_flatten<<<g, kB, 0, s>>>(lab, n);
     NSG_COUNT_LAUNCH();
@@ -703,5 +688,14 @@ extern "C" int nsg_imfill_holes_u8_noalloc(const uint8_t *img, uint8_t *out, int
     select_fill<<<g, kB, 0, s>>>(lab, flag, out, n);
     NSG_COUNT_LAUNCH();
     if (cudaGetLastError() != cudaSuccess) return NSG_ERR_CUDA;
+    // the status word into host stack memory (no pinned buffer: nothing is
+    // allocated); this waits for the stream, so `out` is complete on return
+    int dev_status = 0;
+    if (cudaMemcpyAsync(&dev_status, sc.status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+        cudaGetLastError();
+        return NSG_ERR_CUDA;
+    }
+    if (dev_status & DEV_TIMEOUT) return NSG_ERR_TIMEOUT;
     return NSG_SUCCESS;
 }

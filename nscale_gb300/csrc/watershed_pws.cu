@@ -889,7 +889,10 @@ __device__ __forceinline__ int sfind(int *par, int x) {
         x = p;
     }
 }
-__device__ void sunite(int *par, int a_, int b_) {
+// Domain-group union.  Its retries are bounded; a union abandoned when the
+// bound runs out would leave a wrong flood group, so it sends the flood to
+// the serial path instead (fallback code 14), which needs no groups.
+__device__ void sunite(const PW &a, int *par, int a_, int b_) {
     for (int guard = 0; guard < (1 << 24); ++guard) {
         a_ = sfind(par, a_);
         b_ = sfind(par, b_);
@@ -903,6 +906,7 @@ __device__ void sunite(int *par, int a_, int b_) {
         if (old == a_) return;
         a_ = old;
     }
+    set_fallback(a, 14);
 }
 
 // pocket owners: first domain (or active-shell owner) touching the pocket;
@@ -920,7 +924,7 @@ __global__ void k_pocket_owner(PW a, int *powner) {
             else if (a.st[q] & S_R) set_fallback(a, 7);
             if (d < 0) continue;
             int old = atomicCAS(powner + r, -1, d);
-            if (old != -1 && old != d) sunite(a.sup, old, d);
+            if (old != -1 && old != d) sunite(a, a.sup, old, d);
         }
     }
 }
@@ -936,9 +940,9 @@ __global__ void k_shell_unions(PW a, const int *powner) {
         const int nb[4] = {u - 1, u + 1, u - a.W, u + a.W};
         for (int k = 0; k < 4; ++k) {
             int q = nb[k];
-            if (a.flags[q] & F_FG) sunite(a.sup, o, a.dom[q]);
-            else if (a.st[q] & S_ACTIVE) sunite(a.sup, o, a.uown[q]);
-            else if ((a.st[q] & S_POCKET) && powner[a.proot[q]] >= 0) sunite(a.sup, o, powner[a.proot[q]]);
+            if (a.flags[q] & F_FG) sunite(a, a.sup, o, a.dom[q]);
+            else if (a.st[q] & S_ACTIVE) sunite(a, a.sup, o, a.uown[q]);
+            else if ((a.st[q] & S_POCKET) && powner[a.proot[q]] >= 0) sunite(a, a.sup, o, powner[a.proot[q]]);
         }
     }
 }

@@ -142,6 +142,29 @@ def test_imreconstruct_timeout_is_reported(cuda):
     assert N(out).shape == (512, 512)
 
 
+def test_union_find_timeout_is_reported(cuda):
+    """The union-find's bounded retries report too: with a budget of one step,
+    every cross-tile union on an all-foreground image runs out (its first find
+    walks from a pixel to its tile's root), so bwlabel2 returns NSG_ERR_TIMEOUT
+    instead of partial labels; with the budget restored the same context gives
+    the full answer."""
+    from nscale_gb300 import _lib, morphologic_operations as MO
+    from nscale_gb300.context import get_context
+    img = np.full((256, 256), 255, np.uint8)
+    ctx = get_context(256, 256)
+    ctx.set_spin_budget(1)
+    try:
+        with pytest.raises(_lib.NsgError) as e:
+            MO.bwlabel2(T(img), 8)
+        assert e.value.code == _lib.ERR_TIMEOUT
+        with pytest.raises(_lib.NsgError) as e:
+            MO.imfillHoles(T(255 - img), True, 4)
+        assert e.value.code == _lib.ERR_TIMEOUT
+    finally:
+        ctx.set_spin_budget(0)
+    np.testing.assert_array_equal(N(MO.bwlabel2(T(img), 8)), np.zeros((256, 256), np.int32))
+
+
 @pytest.mark.parametrize("shape", SHAPES + [(1024, 1024)])
 @pytest.mark.parametrize("conn", [4, 8])
 def test_binary_ops(cuda, orc, shape, conn):

@@ -1,7 +1,8 @@
 """nsg_imfill_holes_u8_noalloc: hole filling for callers that cannot allocate
 device memory.  It is checked against nsg_imfill_holes_u8 (the context-based
-entry point) through the C ABI, on consecutive calls that share the library's
-static work array.  This file is collected last so that the test also runs
+entry point) and against the oracle's imfillHoles through the C ABI, on
+consecutive calls that share the library's static work array, and its
+union-find budget is shown to report through its own status word.  This file is collected last so that the test also runs
 after every other test has used the device; it passes when run on its own as
 well."""
 import ctypes as C
@@ -32,7 +33,7 @@ def test_noalloc_rejects_bad_arguments_without_a_device(nsg):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("conn", [4, 8])
-def test_noalloc_matches_context_entry_on_consecutive_calls(cuda, conn):
+def test_noalloc_matches_context_entry_on_consecutive_calls(cuda, orc, conn):
     import torch
     from nscale_gb300 import _lib
     from nscale_gb300.context import get_context, ptr, stream_handle
@@ -59,3 +60,26 @@ def test_noalloc_matches_context_entry_on_consecutive_calls(cuda, conn):
         w, g = want.cpu().numpy(), got.cpu().numpy()
         assert (w == 255).sum() > (img.cpu().numpy() == 255).sum()  # some holes were filled
         assert np.array_equal(g, w), f"case {k} {cases[k]}: {(g != w).sum()} pixels differ"
+        o = orc.imfill_holes(img.cpu().numpy(), conn)
+        assert np.array_equal(g, o), f"case {k} {cases[k]}: {(g != o).sum()} pixels differ from the oracle"
+
+
+@pytest.mark.gpu
+def test_noalloc_timeout_is_reported(cuda, monkeypatch):
+    """With a union-find budget of one step (NSG_SPIN_BUDGET, read at each
+    call: this entry has no context to carry a budget) every cross-tile union
+    on an all-background image runs out; the call returns NSG_ERR_TIMEOUT from
+    its own device status word.  The next call, with the default budget, is
+    complete and correct (everything reached from the border: all zero)."""
+    import torch
+    from nscale_gb300 import _lib
+    from nscale_gb300.context import ptr, stream_handle
+    L = _lib.load()
+    img = torch.zeros((256, 256), dtype=torch.uint8, device="cuda")
+    out = torch.full_like(img, 7)
+    monkeypatch.setenv("NSG_SPIN_BUDGET", "1")
+    assert L.nsg_imfill_holes_u8_noalloc(ptr(img), ptr(out), 256, 256, 4, stream_handle()) == _lib.ERR_TIMEOUT
+    monkeypatch.delenv("NSG_SPIN_BUDGET")
+    assert L.nsg_imfill_holes_u8_noalloc(ptr(img), ptr(out), 256, 256, 4, stream_handle()) == 0
+    torch.cuda.synchronize()
+    assert int(out.max()) == 0
