@@ -1,5 +1,8 @@
 """ctypes wrapper over the CPU oracle (oracle/_build/libnsg_oracle.so) and the
-reference's own ConnComponents (oracle/_ref/libnsg_refcc.so).
+two checkers built from nscale's own code: ConnComponents
+(oracle/_ref/libnsg_refcc.so) and the nscale morphology / pixel functions of
+the segmentNuclei path compiled against an OpenCV stand-in
+(oracle/_ref/libnsg_refnscale.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
 CPU legs of bench.py as the checker.  The product path never imports it.
@@ -15,7 +18,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = os.path.join(HERE, "_build", "libnsg_oracle.so")
 _REF = os.path.join(HERE, "_ref", "libnsg_refcc.so")
-REFERENCE_ROOT = "/root/reference"
+_REFN = os.path.join(HERE, "_ref", "libnsg_refnscale.so")
 
 _u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
@@ -52,14 +55,25 @@ DUMP_TYPES = {"dist": np.float32, "distance2": np.float32, "minima_labels": np.i
               "watermask": np.int32}
 
 
+def nscale_src() -> str:
+    """The nscale source tree: NSCALE_SRC from the environment, else the
+    build recipe's default (oracle/Makefile)."""
+    v = os.environ.get("NSCALE_SRC")
+    if v:
+        return v
+    r = subprocess.run(["make", "-s", "-C", HERE, "nscale-src"], capture_output=True, text=True)
+    return r.stdout.strip()
+
+
 def build(ref: bool | None = None) -> None:
-    """Compile the oracle (and, when the nscale sources are present, the
-    reference's ConnComponents into oracle/_ref)."""
+    """Compile the oracle (and, when the nscale sources are present, the two
+    checkers made from nscale's own code into oracle/_ref)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    src = nscale_src()
     if ref is None:
-        ref = os.path.isdir(os.path.join(REFERENCE_ROOT, "src", "segment"))
+        ref = bool(src) and os.path.isdir(os.path.join(src, "src", "segment"))
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REFERENCE_ROOT}"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"NSCALE_SRC={src}"], check=True)
 
 
 _lib = None
@@ -133,6 +147,62 @@ def ref_lib():
         R.ref_cc_area_threshold.argtypes = [_u8p, C.c_int, C.c_int, _i32p, C.c_int, C.c_int, C.c_int, C.c_int]
         _ref = R
     return _ref
+
+
+_refn = None
+
+
+def refn_lib():
+    """nscale's own morphology / pixel functions (None when not built)."""
+    global _refn
+    if _refn is None and os.path.exists(_REFN):
+        R = C.CDLL(_REFN)
+        for name, args in [
+            ("ref_imreconstruct_u8", [_u8p, _u8p, C.c_int, C.c_int, C.c_int, _u8p]),
+            ("ref_imreconstruct_f32", [_f32p, _f32p, C.c_int, C.c_int, C.c_int, _f32p]),
+            ("ref_imreconstruct_binary_u8", [_u8p, _u8p, C.c_int, C.c_int, C.c_int, _u8p]),
+            ("ref_imfill_holes_u8", [_u8p, C.c_int, C.c_int, C.c_int, _u8p]),
+            ("ref_bwselect_u8", [_u8p, _u8p, C.c_int, C.c_int, C.c_int, _u8p]),
+            ("ref_bwlabel2", [_u8p, C.c_int, C.c_int, C.c_int, _i32p]),
+            ("ref_bwareaopen2", [_u8p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _u8p, C.POINTER(C.c_int)]),
+            ("ref_imhmin_f32", [_f32p, C.c_int, C.c_int, C.c_float, C.c_int, _f32p]),
+            ("ref_border_i32", [_i32p, C.c_int, C.c_int, C.c_int32, _i32p]),
+            ("ref_get_rbc", [_u8p, C.c_int, C.c_int, C.c_double, C.c_double, _u8p]),
+            ("ref_get_background", [_u8p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _u8p]),
+            ("ref_invert_u8", [_u8p, C.c_int, C.c_int, _u8p]),
+            ("ref_invert_i32", [_i32p, C.c_int, C.c_int, _i32p]),
+            ("ref_invert_f32", [_f32p, C.c_int, C.c_int, _f32p]),
+            ("ref_local_minima_f32", [_f32p, C.c_int, C.c_int, C.c_int, _u8p]),
+            ("ref_morph_open_u8", [_u8p, C.c_int, C.c_int, _u8p, C.c_int, _u8p]),
+            ("ref_watershed2", [_u8p, _f32p, C.c_int, C.c_int, C.c_int, _i32p]),
+            ("ref_segment_nuclei", [_u8p, C.c_int, C.c_int] + [C.c_int] * 3 + [C.c_double] * 2 + [C.c_int] * 10
+             + [_i32p, _u8p, _i32p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        ]:
+            f = getattr(R, name)
+            f.argtypes = args
+            f.restype = C.c_int
+        _refn = R
+    return _refn
+
+
+def ref_segment_nuclei(bgr, params: "Params | None" = None):
+    """nscale's own segmentNuclei (both overloads) from oracle/_ref: returns
+    (status, labels, mask, bbox as 5 x n in the reference's own output, i.e.
+    its boundingBox(bgval 0) call, mask-overload status)."""
+    R = refn_lib()
+    p = params or Params()
+    bgr = _c(bgr, np.uint8)
+    rows, cols = bgr.shape[:2]
+    lab = np.full((rows, cols), -1, np.int32)
+    mask = np.zeros((rows, cols), np.uint8)
+    cap = rows * cols // 4 + 16
+    box = np.zeros(5 * cap, np.int32)
+    cc, mst = C.c_int(0), C.c_int(0)
+    st = R.ref_segment_nuclei(bgr, rows, cols, p.blue, p.green, p.red, p.T1, p.T2, p.G1, p.minSize, p.maxSize, p.G2,
+                              p.minSizePl, p.minSizeSeg, p.maxSizeSeg, p.fillHolesConnectivity, p.reconConnectivity,
+                              p.watershedConnectivity, lab, mask, box, cap, C.byref(cc), C.byref(mst))
+    n = cc.value if st == 0 else 0
+    return st, lab, mask, box[:5 * n].reshape(n, 5).T.copy() if n else np.zeros((5, 0), np.int32), mst.value
 
 
 def _c(a, dt):
