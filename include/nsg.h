@@ -100,8 +100,13 @@ int nsg_get_background(nsg_context *ctx, const uint8_t *bgr, int rows, int cols,
  * CPU reference computes it. */
 int nsg_get_rbc(nsg_context *ctx, const uint8_t *bgr, int rows, int cols, double T1, double T2, uint8_t *rbc_out,
                 nsg_stream_t stream);
-/* PixelOperations::invert<unsigned char> (PixelOperations.cpp:22-43). */
+/* PixelOperations::invert<T> (PixelOperations.cpp:22-43) over n elements:
+ * uint8 255 - x; int32 ~x + 1 (two's-complement negation, wrapping at
+ * INT_MIN); float32 -x as the reference's scaled copy x * -1 + 0 (+0 stays
+ * +0).  In-place (in == out) is allowed. */
 int nsg_invert_u8(nsg_context *ctx, const uint8_t *in, uint8_t *out, int64_t n, nsg_stream_t stream);
+int nsg_invert_i32(nsg_context *ctx, const int32_t *in, int32_t *out, int64_t n, nsg_stream_t stream);
+int nsg_invert_f32(nsg_context *ctx, const float *in, float *out, int64_t n, nsg_stream_t stream);
 
 /* ---- MorphologicOperations ------------------------------------------------ */
 /* cv::erode / cv::dilate with a k x k structuring element given in HOST

@@ -81,6 +81,8 @@ _SIGS = {
     "nsg_get_background": (_I, [_P, _P, _I, _I, _I, _I, _I, _P, C.POINTER(C.c_int64), _P]),
     "nsg_get_rbc": (_I, [_P, _P, _I, _I, C.c_double, C.c_double, _P, _P]),
     "nsg_invert_u8": (_I, [_P, _P, _P, C.c_int64, _P]),
+    "nsg_invert_i32": (_I, [_P, _P, _P, C.c_int64, _P]),
+    "nsg_invert_f32": (_I, [_P, _P, _P, C.c_int64, _P]),
     "nsg_morph_erode_u8": (_I, [_P, _P, _P, _I, _I, _P, _I, _P]),
     "nsg_morph_dilate_u8": (_I, [_P, _P, _P, _I, _I, _P, _I, _P]),
     "nsg_morph_open_u8": (_I, [_P, _P, _P, _I, _I, _P, _I, _P]),

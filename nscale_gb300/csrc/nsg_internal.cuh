@@ -194,6 +194,8 @@ int mask_copy_bgr(Ctx &c, const uint8_t *bgr, int64_t row_stride, const uint8_t 
                   uint8_t *out, cudaStream_t s);
 int neg_dist_mask(Ctx &c, const float *dist, const uint8_t *mask, int64_t n, float *out, cudaStream_t s);
 int invert_u8_dev(Ctx &c, const uint8_t *in, uint8_t *out, int64_t n, cudaStream_t s);
+template <typename T>
+int invert_dev(Ctx &c, const T *in, T *out, int64_t n, cudaStream_t s);  // uint8_t, int32_t, float
 // morph.cu
 int morph_u8(Ctx &c, const uint8_t *in, uint8_t *out, int rows, int cols, const uint8_t *se_host, int k,
              bool is_max, cudaStream_t s);

@@ -326,7 +326,21 @@ int nsg_get_rbc(nsg_context *h, const uint8_t *bgr, int rows, int cols, double T
 int nsg_invert_u8(nsg_context *h, const uint8_t *in, uint8_t *out, int64_t n, nsg_stream_t s) {
     return run_op(h, s, [&](Ctx &c) {
         if (!in || !out || n < 0) return NSG_ERR_ARG;
-        return invert_u8_dev(c, in, out, n, S(s));
+        return invert_dev<uint8_t>(c, in, out, n, S(s));
+    });
+}
+
+int nsg_invert_i32(nsg_context *h, const int32_t *in, int32_t *out, int64_t n, nsg_stream_t s) {
+    return run_op(h, s, [&](Ctx &c) {
+        if (!in || !out || n < 0) return NSG_ERR_ARG;
+        return invert_dev<int32_t>(c, in, out, n, S(s));
+    });
+}
+
+int nsg_invert_f32(nsg_context *h, const float *in, float *out, int64_t n, nsg_stream_t s) {
+    return run_op(h, s, [&](Ctx &c) {
+        if (!in || !out || n < 0) return NSG_ERR_ARG;
+        return invert_dev<float>(c, in, out, n, S(s));
     });
 }
 

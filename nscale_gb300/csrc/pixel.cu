@@ -112,9 +112,38 @@ __global__ void neg_dist_mask_kernel(const float *__restrict__ d, const uint8_t 
         out[i] = m[i] ? -d[i] : -FLT_MAX;
 }
 
-__global__ void invert_kernel(const uint8_t *__restrict__ in, uint8_t *__restrict__ out, int64_t n) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        out[i] = (uint8_t)(255 - in[i]);
+// PixelOperations::invert<T> (PixelOperations.cpp:22-43): unsigned
+// max - x, signed ~x + 1 (two's-complement negation, wrapping), float -x as
+// the reference's scaled copy x * -1 + 0 (so +0 stays +0)
+__device__ __forceinline__ uint8_t inv1(uint8_t v) { return (uint8_t)(255 - v); }
+__device__ __forceinline__ int32_t inv1(int32_t v) { return (int32_t)(~(uint32_t)v + 1u); }
+__device__ __forceinline__ float inv1(float v) { return __fadd_rn(__fmul_rn(v, -1.0f), 0.0f); }
+
+// 16 bytes per thread and step when both arrays are 16-byte aligned (the
+// grid strides over 16-byte words, consecutive lanes on consecutive words),
+// the remainder one element per thread
+template <typename T>
+__global__ void invert_kernel(const T *__restrict__ in, T *__restrict__ out, int64_t n, int vec) {
+    constexpr int K = 16 / sizeof(T);
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
+    int64_t done = 0;
+    if (vec) {
+        const int64_t nw = n / K;
+        const uint4 *src = reinterpret_cast<const uint4 *>(in);
+        uint4 *dst = reinterpret_cast<uint4 *>(out);
+        for (int64_t w = tid; w < nw; w += nth) {
+            union {
+                uint4 u;
+                T e[K];
+            } a;
+            a.u = __ldg(src + w);
+#pragma unroll
+            for (int k = 0; k < K; ++k) a.e[k] = inv1(a.e[k]);
+            dst[w] = a.u;
+        }
+        done = nw * K;
+    }
+    for (int64_t i = done + tid; i < n; i += nth) out[i] = inv1(in[i]);
 }
 
 }  // namespace
@@ -179,11 +208,21 @@ int neg_dist_mask(Ctx &c, const float *d, const uint8_t *m, int64_t n, float *ou
     return NSG_SUCCESS;
 }
 
-int invert_u8_dev(Ctx &c, const uint8_t *in, uint8_t *out, int64_t n, cudaStream_t s) {
-    invert_kernel<<<blocks_for(c, n), kBlock, 0, s>>>(in, out, n);
+template <typename T>
+int invert_dev(Ctx &c, const T *in, T *out, int64_t n, cudaStream_t s) {
+    const int vec = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
+    const int64_t work = vec ? (n * (int64_t)sizeof(T) + 15) / 16 : n;
+    invert_kernel<T><<<blocks_for(c, work), kBlock, 0, s>>>(in, out, n, vec);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
+}
+template int invert_dev<uint8_t>(Ctx &, const uint8_t *, uint8_t *, int64_t, cudaStream_t);
+template int invert_dev<int32_t>(Ctx &, const int32_t *, int32_t *, int64_t, cudaStream_t);
+template int invert_dev<float>(Ctx &, const float *, float *, int64_t, cudaStream_t);
+
+int invert_u8_dev(Ctx &c, const uint8_t *in, uint8_t *out, int64_t n, cudaStream_t s) {
+    return invert_dev<uint8_t>(c, in, out, n, s);
 }
 
 }  // namespace nsg

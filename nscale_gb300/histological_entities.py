@@ -116,13 +116,15 @@ class PixelOperations:
 
     @staticmethod
     def invert(img: torch.Tensor) -> torch.Tensor:
-        """PixelOperations.cpp:22-43 (uint8: 255 - x)."""
-        if img.dtype != torch.uint8:
-            raise TypeError("the GPU invert on the path is uint8")
+        """PixelOperations::invert<T> (PixelOperations.cpp:22-43): uint8
+        255 - x, int32 ~x + 1, float32 -x."""
+        fn = {torch.uint8: "nsg_invert_u8", torch.int32: "nsg_invert_i32", torch.float32: "nsg_invert_f32"}
+        if img.dtype not in fn:
+            raise TypeError("invert takes uint8, int32 or float32 (the reference's instantiations on the path)")
         img = img.contiguous()
-        ctx = get_context(1, max(1, img.numel()))
+        ctx = get_context(1, 1)
         out = torch.empty_like(img)
-        ctx.check(ctx.L.nsg_invert_u8(ctx.h, ptr(img), ptr(out), img.numel(), stream_handle()))
+        ctx.check(getattr(ctx.L, fn[img.dtype])(ctx.h, ptr(img), ptr(out), img.numel(), stream_handle()))
         return out
 
 

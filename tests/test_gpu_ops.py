@@ -382,3 +382,56 @@ def test_gradient_and_nucleus_features(cuda, orc, shape):
     assert np.array_equal(got[:, 0], want[:, 0])
     assert np.allclose(got[:, 1], want[:, 1], rtol=1e-6, atol=0)
     assert np.array_equal(got[:, 2:], want[:, 2:])
+
+
+@pytest.mark.parametrize("n", [1, 15, 16, 17, 4099, 1 << 20])
+def test_invert_all_types(cuda, n):
+    """PixelOperations::invert<T> for the three instantiations, on lengths
+    around the 16-byte vector width and on views that start off a 16-byte
+    boundary (element tail path)."""
+    import torch
+    from nscale_gb300.histological_entities import HistologicalEntities as HE
+    g = np.random.default_rng(n)
+    u8 = g.integers(0, 256, size=n + 3).astype(np.uint8)
+    i32 = g.integers(-2 ** 31, 2 ** 31, size=n + 3, dtype=np.int64).astype(np.int32)
+    i32[0] = np.iinfo(np.int32).min  # ~x + 1 wraps there, as the reference's int arithmetic
+    f32 = g.standard_normal(n + 3).astype(np.float32)
+    f32[:2] = (0.0, -0.0)
+    for a, want in ((u8, (255 - u8).astype(np.uint8)), (i32, (~i32 + np.int32(1)).astype(np.int32)),
+                    (f32, (-f32 + np.float32(0)).astype(np.float32))):
+        t = torch.from_numpy(a).cuda()
+        for off in (0, 1):
+            got = N(HE.invert(t[off:off + n]))
+            assert got.dtype == a.dtype
+            np.testing.assert_array_equal(got, want[off:off + n])
+    with pytest.raises(TypeError):
+        HE.invert(torch.zeros(4, dtype=torch.float64, device="cuda"))
+
+
+def test_segment_nuclei_host_entry(cuda, orc):
+    """nsg_segment_nuclei_host (host buffers in and out, the entry a C++
+    caller without device memory uses) against the oracle."""
+    import ctypes as C
+    from nscale_gb300 import _lib, synth
+    from nscale_gb300.context import get_context, stream_handle
+    img = np.ascontiguousarray(synth.he_tile(300, 517, seed=0x5EED0003))
+    rows, cols = img.shape[:2]
+    ctx = get_context(rows, cols)
+    lab = np.empty((rows, cols), np.int32)
+    mask = np.empty((rows, cols), np.uint8)
+    cc = C.c_int(0)
+    bbox = C.POINTER(C.c_int32)()
+    st = ctx.L.nsg_segment_nuclei_host(ctx.h, img.ctypes.data, rows, cols, None, lab.ctypes.data, mask.ctypes.data,
+                                       C.byref(cc), C.byref(bbox), stream_handle())
+    ost, olab, omask, obox, _ = orc.segment_nuclei(img)
+    assert st == ost == 0
+    np.testing.assert_array_equal(lab, olab)
+    np.testing.assert_array_equal(mask, omask)
+    boxes = np.ctypeslib.as_array(bbox, shape=(5 * cc.value,)).reshape(5, cc.value).copy()
+    ctx.L.nsg_free(bbox)
+    np.testing.assert_array_equal(boxes, obox)
+    # a tile larger than the context is refused, nothing is written
+    big = get_context(rows, cols)
+    st = big.L.nsg_segment_nuclei_host(big.h, img.ctypes.data, big.max_rows + 1, big.max_cols + 1, None, None,
+                                       None, None, None, stream_handle())
+    assert st == _lib.ERR_OOM
