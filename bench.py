@@ -8,10 +8,13 @@ reference's validation slides are not available).  One step = the full
 segmentNuclei pipeline over every tile of the batch through libnsg.so's
 batched entry point (nsg_segment_nuclei_batch: a pool of workers, each with
 its own context and stream, keeps several tiles in flight), inputs resident in
-HBM.  Inputs (1.9 Gpixel, 5.6 GB) are far larger than L2.  Also reported: the
-same tiles through plain per-tile calls on one stream (the batched speed-up),
-per-stage times, the host-buffer end-to-end rate, and p50/p99 latency of a
-short Poisson-arrival run through the in-process server (nsg_server_*).
+HBM.  Inputs (1.9 Gpixel, 5.6 GB) are far larger than L2.  Also reported, on
+the same tiles: plain per-tile calls on one stream (the batched speed-up),
+per-stage times, the host-buffer end-to-end rate, and a parity check of the
+batched labels against the oracle on the CPU-baseline sample; then the
+serving form: Poisson arrivals of tiles cut from a synthetic 100000 x 80000
+slide into the in-process server (nsg_server_*), swept over arrival rates,
+with p50/p99 latency, throughput and shed requests per rate.
 
 Prints ONE JSON line (rank 0).  `--impl reference` times the reference's CPU
 segmentNuclei path instead: the CPU oracle (a restatement of the reference;
@@ -30,6 +33,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -62,12 +66,15 @@ def parse():
     ap.add_argument("--tiles", type=int, default=256)
     ap.add_argument("--streams", type=int, default=32,
                     help="tiles in flight: pool workers, each with its own context and CUDA stream")
-    ap.add_argument("--per-tile-tiles", type=int, default=64, help="tiles timed in the per-tile comparison")
     ap.add_argument("--autotune-tiles", type=int, default=96,
                     help="tiles of the batch the autotuner measures launch shapes on (0 = defaults)")
-    ap.add_argument("--serve-tiles", type=int, default=96, help="tiles sent through the server (0 = skip)")
-    ap.add_argument("--serve-load", default="0.3,0.7,0.95",
-                    help="offered loads to sweep, fractions of the batched throughput (comma list)")
+    ap.add_argument("--serve-requests", type=int, default=1000,
+                    help="slide-tile requests per arrival rate in the serving sweep (0 = skip)")
+    ap.add_argument("--serve-rates", default="50,100,200,500,1000,2000",
+                    help="Poisson arrival rates to sweep, tiles/s (comma list)")
+    ap.add_argument("--serve-distinct", type=int, default=64, help="distinct slide positions the requests visit")
+    ap.add_argument("--serve-queue", type=int, default=128, help="waiting tiles before the server sheds")
+    ap.add_argument("--serve-budget-gib", type=int, default=160, help="device memory the server's workers may hold")
     ap.add_argument("--cpu-sample-tiles", type=int, default=0, help="tiles in the CPU baseline sample (0 = cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -112,7 +119,8 @@ class Clocks:
     def __init__(self, dev):
         self.dev = dev
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        d = os.environ.get("NSG_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(d, f"nsg_clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
@@ -166,20 +174,31 @@ def make_batch(n_tiles, seed_base, device):
     return tiles
 
 
+def labels_digest(status, labels) -> str:
+    """Status and int32 label image of one tile as a short digest (parity
+    check of the benchmarked tiles against the oracle's)."""
+    import hashlib
+    import numpy as np
+    h = hashlib.sha256(str(int(status)).encode())
+    h.update(np.ascontiguousarray(labels, dtype=np.int32).tobytes())
+    return h.hexdigest()[:20]
+
+
 def cpu_worker(args):
-    """One oracle segmentNuclei (spawned process)."""
+    """One oracle segmentNuclei (spawned process): (seconds, digest)."""
     import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     tile = np.frombuffer(args[0], dtype=np.uint8).reshape(args[1], args[2], 3)
     t = time.perf_counter()
-    oracle.segment_nuclei(tile)
-    return time.perf_counter() - t
+    st, lab, _, _, _ = oracle.segment_nuclei(tile)
+    dt = time.perf_counter() - t
+    return dt, labels_digest(st, lab)
 
 
 def cpu_throughput(tiles_np, procs):
     """Oracle segmentNuclei over `tiles_np` with `procs` spawned workers;
-    returns (Mpixel/s, wall seconds)."""
+    returns (Mpixel/s, wall seconds, per-tile digests)."""
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
     payload = [(t.tobytes(), t.shape[0], t.shape[1]) for t in tiles_np]
@@ -187,9 +206,9 @@ def cpu_throughput(tiles_np, procs):
     with ctx.Pool(procs) as pool:
         pool.map(cpu_worker, payload[:procs])  # warm the workers (imports, oracle build check)
         t = time.perf_counter()
-        pool.map(cpu_worker, payload)
+        res = pool.map(cpu_worker, payload)
         wall = time.perf_counter() - t
-    return px / wall / 1e6, wall
+    return px / wall / 1e6, wall, [d for _, d in res]
 
 
 def run_reference(args, rank, world):
@@ -211,7 +230,7 @@ def run_reference(args, rank, world):
     px = sum(t.shape[0] * t.shape[1] for t in sample)
     vals = []
     for i in range(args.warmup + args.steps):
-        v, wall = cpu_throughput(sample, min(cores, len(sample)))
+        v, wall, _ = cpu_throughput(sample, min(cores, len(sample)))
         if i >= args.warmup:
             vals.append((v, wall))
     value = statistics.mean(v for v, _ in vals)
@@ -235,7 +254,7 @@ def run_nsg(args, rank, world, local):
     import torch
     from nscale_gb300 import _lib
     from nscale_gb300.context import Context, ptr
-    from nscale_gb300.serving import TilePool, TileServer
+    from nscale_gb300.serving import TilePool
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     L = _lib.load()
@@ -267,16 +286,20 @@ def run_nsg(args, rank, world, local):
     # ---- batched form: every tile of the batch on the pool's workers --------
     tuning = None
     if args.autotune_tiles > 0:
-        # launch shapes picked on the first tiles of the batch (results do not depend on them)
+        # launch shapes picked on calibration tiles that are not the timed
+        # batch (same generator and size mix, other seeds); the choice is
+        # cached per GPU and tile-size mix.  Results do not depend on it.
         from nscale_gb300.autotune import autotune
-        tuning = autotune(tiles[: args.autotune_tiles], device=local)
+        calib = make_batch(args.autotune_tiles, 0x5EEDCA11, dev)
+        tuning = autotune(calib, device=local)
+        del calib
         args.streams = tuning["workers"]
     else:
         from nscale_gb300.autotune import max_workers
         args.streams = min(args.streams, max_workers(maxr, maxc, local))
     pool = TilePool(maxr, maxc, workers=max(1, args.streams), device=local)
     if tuning:
-        pool.set_tuning(tuning["recon_max_ctas"], tuning["bfs_max_cluster"])
+        pool.set_tuning(tuning["recon_max_ctas"], tuning["bfs_max_cluster"], tuning["recon_wl_phases"])
     labels = [torch.empty(t.shape[0] * t.shape[1], dtype=torch.int32, device=dev) for t in tiles]
     arr = (_lib.Tile * len(tiles))()
     for i, t in enumerate(tiles):
@@ -299,26 +322,23 @@ def run_nsg(args, rank, world, local):
         statuses[arr[i].status] = statuses.get(arr[i].status, 0) + 1
     value, ms_step = replica_rate(px, total_ms / args.steps, world, dev)
 
-    # ---- e2e: host (pinned) tiles in, labels back to pinned host memory,
-    # through the same batched entry point; copies inside the timed region
-    e2e_tiles = tiles[: min(len(tiles), 64)]
-    host_in = [t.cpu().pin_memory() for t in e2e_tiles]
-    host_lab = [torch.empty(t.shape[0] * t.shape[1], dtype=torch.int32).pin_memory() for t in e2e_tiles]
+    # ---- e2e: the same tiles from pinned host memory, labels back to pinned
+    # host memory, through the same batched entry point; copies inside the
+    # timed region
+    host_in = [t.cpu().pin_memory() for t in tiles]
+    host_lab = [torch.empty(t.shape[0] * t.shape[1], dtype=torch.int32).pin_memory() for t in tiles]
     harr = (_lib.Tile * len(host_in))()
     for i, h in enumerate(host_in):
         harr[i].bgr, harr[i].rows, harr[i].cols, harr[i].row_stride_bytes = h.data_ptr(), h.shape[0], h.shape[1], 0
         harr[i].labels, harr[i].mask, harr[i].want_bbox = host_lab[i].data_ptr(), None, 0
-    e2e_px = sum(t.shape[0] * t.shape[1] for t in e2e_tiles)
     pool.run(harr, params, host=True)
-    e2e_ms = event_time(lambda: [pool.run(harr, params, host=True) for _ in range(args.steps)]) / args.steps
-    e2e_value, _ = replica_rate(e2e_px, e2e_ms, world, dev)
+    e2e_steps = max(1, min(args.steps, 3))
+    e2e_ms = event_time(lambda: [pool.run(harr, params, host=True) for _ in range(e2e_steps)]) / e2e_steps
+    e2e_value, _ = replica_rate(px, e2e_ms, world, dev)
     pool.close()
 
     # ---- per-tile form: the same tiles one call at a time on one stream,
     # with per-stage CUDA-event timing (the stage table below)
-    n_pt = min(len(tiles), args.per_tile_tiles)
-    pt_tiles = tiles[:n_pt]
-    pt_px = sum(t.shape[0] * t.shape[1] for t in pt_tiles)
     ctx = Context(maxr, maxc, local)
     stream = torch.cuda.Stream(device=dev)
     sh = C.c_void_p(stream.cuda_stream)
@@ -327,7 +347,7 @@ def run_nsg(args, rank, world, local):
     tile_ms = []
 
     def per_tile(record=False):
-        for t in pt_tiles:
+        for t in tiles:
             t0 = time.perf_counter()
             st = L.nsg_segment_nuclei(ctx.h, ptr(t), t.shape[0], t.shape[1], t.shape[1] * 3, C.byref(params),
                                       ptr(lab1), None, C.byref(cc), None, sh)
@@ -355,24 +375,35 @@ def run_nsg(args, rank, world, local):
         per_tile(record=True)  # latency of one tile alone
     names = [L.nsg_stage_name(i).decode() for i in range(n_stages)]
     per_stage = {names[i]: stage_ms[i] for i in range(n_stages)}
-    pt_value = pt_px / (pt_ms / 1e3) / 1e6
+    pt_value = px / (pt_ms / 1e3) / 1e6
     ctx.close()
 
-    # ---- serving: Poisson arrivals of host tiles into the server ------------
+    # ---- serving: Poisson arrivals of slide tiles into the server -----------
     serving = None
-    if rank == 0 and args.serve_tiles > 0:
-        serving = serve(args, tiles, value / world)
+    if rank == 0 and args.serve_requests > 0:
+        serving = serve(args, local)
 
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         n = args.cpu_sample_tiles or cores
         sample = [t.cpu().numpy() for t in tiles[:n]]
-        v, wall = cpu_throughput(sample, min(cores, len(sample)))
+        v, wall, digests = cpu_throughput(sample, min(cores, len(sample)))
         spx = sum(t.shape[0] * t.shape[1] for t in sample)
         cpu = {"value": round(v, 3), "unit": "Mpixel/s", "cores": min(cores, len(sample)), "kind": "port",
                "sample": f"{len(sample)} tiles of the batch ({spx / 1e6:.1f} Mpixel), one tile per process, "
                          f"{wall:.1f} s"}
+        # the batched form's labels of the same tiles (last timed pass) against the oracle's
+        bad = []
+        for i in range(len(sample)):
+            got = labels[i].view(tiles[i].shape[0], tiles[i].shape[1]).cpu().numpy()
+            if arr[i].status != 0:
+                got = np.full(got.shape, -1, np.int32)
+            if labels_digest(arr[i].status, got) != digests[i]:
+                bad.append(i)
+        parity = {"tiles": len(sample), "mismatches": len(bad), "mismatched_tiles": bad,
+                  "what": "status + int32 labels of the batched run vs the oracle, per tile (SHA-256)"}
 
     if rank != 0:
         return
@@ -388,16 +419,19 @@ def run_nsg(args, rank, world, local):
                    "tiles": len(tiles), "pixels_per_step": px,
                    "form": f"batched: nsg_segment_nuclei_batch, {pool_workers(args)} tiles in flight "
                            f"(one context and stream per worker)",
-                   "tuning": ({k: tuning[k] for k in ("workers", "recon_max_ctas", "bfs_max_cluster")}
-                              | {"picked_from": len(tuning["trials"]), "calibration_tiles": tuning["calibration_tiles"]}
+                   "tuning": ({k: tuning[k] for k in ("workers", "recon_max_ctas", "bfs_max_cluster",
+                                                     "recon_wl_phases")}
+                              | {"picked_from": len(tuning["trials"]), "calibration_tiles": tuning["calibration_tiles"],
+                                 "cached": tuning.get("cached", False)}
                               if tuning else "defaults"),
                    "l2": "inputs larger than L2 (5.6 GB per step)", "parallelism": f"replicas x{world}"},
-        "per_tile": {"value": round(pt_value, 3), "unit": "Mpixel/s", "tiles": n_pt,
-                     "form": "nsg_segment_nuclei one tile at a time on one stream",
+        "per_tile": {"value": round(pt_value, 3), "unit": "Mpixel/s", "tiles": len(tiles),
+                     "form": "nsg_segment_nuclei one tile at a time on one stream, the same tiles",
                      "batched_speedup": round(value / world / pt_value, 2)},
         "latency_ms": {"p50": round(lat[len(lat) // 2], 3),
                        "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3),
-                       "what": "one tile alone, per-tile form"},
+                       "max": round(lat[-1], 3), "samples": len(lat),
+                       "what": "one tile alone, per-tile form (host clock, submit to stream drained)"},
         "statuses": {str(k): v for k, v in statuses.items()},
         "stage_ms_per_tile_pass": {k: round(v, 3) for k, v in per_stage.items() if v > 0},
         "stage_ms_per_tile_batched": {k: round(v / max(1, batched_timed), 3)
@@ -409,11 +443,14 @@ def run_nsg(args, rank, world, local):
                      "traffic": int(DRAM_BYTES_PER_PX * px),
                      "traffic_note": f"DRAM bytes per step: {DRAM_BYTES_PER_PX} B/px measured by ncu over all "
                                      f"kernels of one 2048x2048 tile, x pixels per step"},
-        "e2e": {"value": round(e2e_value, 3), "unit": "Mpixel/s", "h2d_bytes_per_step": int(3 * e2e_px),
-                "d2h_bytes_per_step": int(4 * e2e_px), "tiles": len(e2e_tiles)},
+        "e2e": {"value": round(e2e_value, 3), "unit": "Mpixel/s", "h2d_bytes_per_step": int(3 * px),
+                "d2h_bytes_per_step": int(4 * px), "tiles": len(tiles),
+                "form": "the same tiles from pinned host memory through nsg_segment_nuclei_batch (NSG_TILE_HOST)"},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
+    if parity:
+        line["parity"] = parity
     if serving:
         line["serving"] = serving
     if cpu:
@@ -425,65 +462,98 @@ def pool_workers(args):
     return max(1, args.streams)
 
 
-def serve(args, tiles, batched_mpx_s):
-    """Poisson arrivals of host tiles into nsg_server at `serve_load` x the
-    batched throughput, every fifth tile tissue-free (near-white: the
-    BACKGROUND early exit), each result carrying the per-nucleus features of
-    its H channel; returns latency percentiles (submit -> result)."""
-    import numpy as np
+def serve(args, device):
+    """Serving form on the slide workload: tile requests cut from a synthetic
+    100000 x 80000 slide (4096-px tiles, ragged right / bottom edges, 20 %
+    tissue-free), Poisson arrivals at each rate of --serve-rates, at least
+    --serve-requests requests per rate.  The server's workers are in two size
+    classes (full 4096 x 4096 tiles and edge tiles up to 4096 x 2176 / 1696 x
+    4096), bought from a device-memory budget; a full queue (--serve-queue
+    waiting tiles) rejects a request, which is counted as shed.  Each result
+    carries the per-nucleus features of its H channel.  Latency = submit ->
+    result, over the admitted requests."""
     import random
-    from nscale_gb300 import _lib, synth
+    import numpy as np
+    import torch
+    from nscale_gb300 import _lib
     from nscale_gb300.serving import TileServer
-    sub = tiles[: args.serve_tiles]
-    mr = max(t.shape[0] for t in sub)
-    mc = max(t.shape[1] for t in sub)
-    white = synth.white_tile(mr, mc, 0x5EED0004)  # cut to each tile's shape
-    host = [t.cpu().numpy() if i % 5 != 4 else np.ascontiguousarray(white[: t.shape[0], : t.shape[1]])
-            for i, t in enumerate(sub)]
-    labs = [np.empty(h.shape[:2], np.int32) for h in host]
-    maxr = max(h.shape[0] for h in host)
-    maxc = max(h.shape[1] for h in host)
-    per = _lib.load().nsg_pool_context_bytes(maxr, maxc)
-    srv = TileServer(maxr, maxc, memory_budget_bytes=per * max(1, args.streams), queue_cap=len(host))
-    mean_px = sum(h.shape[0] * h.shape[1] for h in host) / len(host)
+    from nscale_gb300.slide import SyntheticSlide
+    slide = SyntheticSlide(80000, 100000, 4096, seed=0x5EED0004)
+    # the distinct tile positions the request stream visits, cut from the
+    # slide before the timed runs (pinned host buffers, as a tiler would hand
+    # them over); requests cycle over them in a shuffled order
+    rng = random.Random(0x5EED0004)
+    positions = [slide.position(k) for k in range(len(slide))]
+    rng.shuffle(positions)
+    positions = positions[: args.serve_distinct]
+    host = []
+    for (i, j) in positions:
+        t = slide.tile(i, j, device=f"cuda:{device}")
+        host.append(t.cpu().pin_memory().numpy())
+        del t
+    torch.cuda.synchronize()
+    L = _lib.load()
+    edge = (max(slide.rows - (slide.grid[0] - 1) * 4096, slide.cols - (slide.grid[1] - 1) * 4096), 4096)
+    classes = [(4096, 4096), (4096, max(edge[0], 2176))]  # full tiles; ragged edge tiles (either orientation)
+    # weights ~ the share of request pixels of each class
+    full = sum(1 for h in host if h.shape[0] == 4096 and h.shape[1] == 4096)
+    weights = [max(1.0, full), max(1.0, len(host) - full)]
+    budget = args.serve_budget_gib << 30
+    srv = TileServer(0, 0, budget, queue_cap=args.serve_queue, device=device, classes=classes, weights=weights)
+    workers = srv.workers
+    class_workers = {f"{r}x{c}": n for (r, c), n in srv.class_workers().items()}
     # warm-up: every worker runs tiles once (first-use set-up stays out of the latencies)
-    warm = min(len(host), 2 * srv.workers)
-    for h, lab in zip(host[:warm], labs[:warm]):
-        srv.submit(h, lab, want_features=True)
+    warm = min(len(host), 2 * workers)
+    for h in host[:warm]:
+        srv.submit(h, None, want_features=True)
     got = 0
     while got < warm:
         got += len(srv.poll(64, 100))
     runs = []
-    for load in [float(x) for x in str(args.serve_load).split(",") if x]:
-        rate = load * batched_mpx_s * 1e6 / mean_px  # tiles per second
-        rng = random.Random(0x5EED0004)
-        results = []
+    n_req = args.serve_requests
+    for rate in [float(x) for x in str(args.serve_rates).split(",") if x]:
+        arrivals = random.Random(int(rate) * 7919)
+        results, shed = [], 0
         t0 = time.perf_counter()
         due = t0
-        for h, lab in zip(host, labs):
-            due += rng.expovariate(rate)
-            while time.perf_counter() < due:
+        for k in range(n_req):
+            due += arrivals.expovariate(rate)
+            while True:
+                now = time.perf_counter()
+                if now >= due:
+                    break
                 results += srv.poll(64, 0)
-                time.sleep(min(0.0005, max(0.0, due - time.perf_counter())))
-            srv.submit(h, lab, want_features=True)
-        while len(results) < len(host):
+                time.sleep(min(0.0005, due - now))
+            try:
+                srv.submit(host[k % len(host)], None, want_features=True)
+            except _lib.NsgError as e:
+                if e.code != _lib.ERR_QUEUE_FULL:
+                    raise
+                shed += 1
+        while len(results) < n_req - shed:
             results += srv.poll(64, 100)
         wall = time.perf_counter() - t0
         lat = sorted(r["latency_ms"] for r in results)
         st = {}
         for r in results:
             st[str(r["status"])] = st.get(str(r["status"]), 0) + 1
+        done_px = sum(host[k % len(host)].shape[0] * host[k % len(host)].shape[1] for k in range(len(results)))
         nfeat = sum(len(r["features"]) for r in results if r["features"] is not None)
-        runs.append({"load": load, "offered_tiles_per_s": round(rate, 2),
-                     "achieved_tiles_per_s": round(len(host) / wall, 2),
-                     "achieved_mpx_s": round(sum(h.shape[0] * h.shape[1] for h in host) / wall / 1e6, 2),
-                     "p50_ms": round(lat[len(lat) // 2], 3),
-                     "p99_ms": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3),
+        runs.append({"offered_tiles_per_s": rate, "requests": n_req, "admitted": len(results), "shed": shed,
+                     "achieved_tiles_per_s": round(len(results) / wall, 2),
+                     "achieved_mpx_s": round(done_px / wall / 1e6, 2),
+                     "p50_ms": round(lat[len(lat) // 2], 3) if lat else None,
+                     "p99_ms": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3) if lat else None,
                      "statuses": st, "nuclei_with_features": nfeat})
-    workers = srv.workers
     srv.close()
-    return {"tiles_per_run": len(host), "arrivals": "poisson", "workers": workers,
-            "output": "labels + per-nucleus area, perimeter, mean/std H, mean gradient; every 5th tile tissue-free",
+    return {"slide": f"{slide.cols}x{slide.rows} synthetic, {slide.tile_size}-px tiles "
+                     f"({slide.grid[1]}x{slide.grid[0]} grid, ragged edges, {slide.tissue_free:.0%} tissue-free), "
+                     f"{len(host)} distinct positions cut before the runs",
+            "arrivals": "poisson", "workers": workers, "class_workers": class_workers,
+            "budget_gib": args.serve_budget_gib, "queue_cap": args.serve_queue,
+            "policy": "admit while fewer than queue_cap tiles wait, else shed (submit returns NSG_ERR_QUEUE_FULL); "
+                      "a worker takes the oldest waiting tile of its size class first",
+            "output": "per-nucleus area, perimeter, mean/std H, mean gradient",
             "runs": runs}
 
 

@@ -83,10 +83,15 @@ int nsg_context_set_spin_budget(nsg_context *ctx, long long iterations);
  * fixed shapes): results do not depend on it.  recon_max_ctas caps the
  * grey reconstruction's persistent grid (0 = one CTA per SM);
  * bfs_max_cluster is the largest thread-block cluster the watershed BFS
- * tries (1-16, 0 = 16).  nscale_gb300.autotune measures and picks them. */
+ * tries (1-16, 0 = 16); recon_wl_phases is the reconstruction's switchover
+ * from scans to its in-tile pixel queue: 0 = row / column phase pairs until
+ * a tile is stable, k = 1..8 = k phase pairs, then the pixel worklist
+ * (-1 = the library default).  nscale_gb300.autotune measures and picks
+ * them. */
 typedef struct nsg_tuning {
     int recon_max_ctas;
     int bfs_max_cluster;
+    int recon_wl_phases;
 } nsg_tuning;
 int nsg_context_set_tuning(nsg_context *ctx, const nsg_tuning *t);
 
@@ -315,7 +320,21 @@ typedef struct nsg_result {
 size_t nsg_pool_context_bytes(int max_rows, int max_cols);
 int nsg_server_create(nsg_server **srv, int max_rows, int max_cols, size_t memory_budget_bytes, int queue_cap,
                       int device);
+/* The same server with workers in size classes: class k holds tiles up to
+ * class_rows[k] x class_cols[k] (one context of nsg_pool_context_bytes each).
+ * The budget is split in proportion to weights[k] x bytes[k] (NULL = equal
+ * weights), at least one worker of the largest class, at most 64 workers.
+ * A submitted tile may run on any worker whose context holds it; a worker
+ * takes the oldest waiting tile of its own class first, else the oldest one
+ * it can hold.  Submit returns NSG_ERR_OOM for a tile no class holds and
+ * NSG_ERR_QUEUE_FULL while queue_cap tiles wait (the caller's shedding
+ * point).  No counterpart in the reference, which farms one tile per MPI
+ * process (nu-segment.cpp:274-430). */
+int nsg_server_create_classes(nsg_server **srv, const int *class_rows, const int *class_cols, const double *weights,
+                              int nclasses, size_t memory_budget_bytes, int queue_cap, int device);
 int nsg_server_workers(const nsg_server *srv);
+/* workers whose context is exactly max_rows x max_cols */
+int nsg_server_class_workers(const nsg_server *srv, int max_rows, int max_cols);
 /* `tile` is copied (its pointers are not); *ticket identifies the result */
 int nsg_server_submit(nsg_server *srv, const nsg_tile *tile, const nsg_seg_params *p, long long *ticket);
 /* up to max finished results, waiting up to wait_ms for the first; returns

@@ -46,7 +46,7 @@ class SegParams(C.Structure):
 class Tuning(C.Structure):
     """nsg_tuning: launch shapes (results do not depend on them)."""
 
-    _fields_ = [("recon_max_ctas", C.c_int), ("bfs_max_cluster", C.c_int)]
+    _fields_ = [("recon_max_ctas", C.c_int), ("bfs_max_cluster", C.c_int), ("recon_wl_phases", C.c_int)]
 
 
 class Tile(C.Structure):
@@ -104,6 +104,9 @@ _SIGS = {
     "nsg_segment_nuclei_batch": (_I, [_P, C.POINTER(Tile), _I, C.POINTER(SegParams), _I]),
     "nsg_server_create": (_I, [C.POINTER(_P), _I, _I, C.c_size_t, _I, _I]),
     "nsg_server_workers": (_I, [_P]),
+    "nsg_server_create_classes": (_I, [C.POINTER(_P), C.POINTER(_I), C.POINTER(_I), C.POINTER(C.c_double), _I,
+                                       C.c_size_t, _I, _I]),
+    "nsg_server_class_workers": (_I, [_P, _I, _I]),
     "nsg_server_submit": (_I, [_P, C.POINTER(Tile), C.POINTER(SegParams), C.POINTER(C.c_longlong)]),
     "nsg_server_poll": (_I, [_P, C.POINTER(Result), _I, _I]),
     "nsg_server_destroy": (_I, [_P]),

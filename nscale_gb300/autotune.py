@@ -1,17 +1,26 @@
 """Autotuner for the batched form: measures nsg_segment_nuclei_batch on a
-calibration batch for a small grid of launch shapes — tiles in flight
-(workers), the reconstruction's persistent grid (as a fraction of the SMs)
-and the largest BFS cluster — and returns the fastest.  Results do not
-depend on these shapes, only the throughput does.
+calibration batch (tiles of the same generator and size mix as the workload,
+not the timed tiles) over the knobs that set its speed — tiles in flight
+(workers), the reconstruction's persistent grid (a fraction of the SMs), the
+reconstruction's scan-to-queue switchover (phase pairs until a tile is
+stable, or k phase pairs and then the in-tile pixel worklist) and the largest
+BFS cluster — and returns the fastest.  Results do not depend on any of them,
+only the throughput does.
 
-    python -m nscale_gb300.autotune [--tiles 32] [--out tuning.json]
+Search: every (workers, grid) pair once, the three best again with `reps`
+CUDA-event-timed repetitions, then the switchover options at the best pair.
+The choice is cached in a JSON file keyed by the GPU (name, SM count) and the
+calibration batch's size mix, so a later run on the same GPU and mix reuses
+it (NSG_AUTOTUNE_CACHE names the file; default ~/.cache/nsg/autotune.json).
+
+    python -m nscale_gb300.autotune [--tiles 96] [--out tuning.json]
 """
 from __future__ import annotations
 
 import argparse
-import itertools
+import hashlib
 import json
-import time
+import os
 
 import torch
 
@@ -21,6 +30,7 @@ from .serving import TilePool
 WORKERS = (24, 32, 40)
 RECON_FRACTIONS = (1 / 32, 1 / 16, 1 / 8)
 BFS_CLUSTERS = (16,)
+RECON_SWITCHOVER = (0, 2, 3)  # 0: phase pairs until stable; k: k pairs, then the pixel worklist
 
 
 def _tile_array(tiles):
@@ -43,10 +53,45 @@ def max_workers(max_rows: int, max_cols: int, device: int = 0, reserve: float = 
     return max(1, int(usable // per)) if per > 0 else 1
 
 
-def autotune(tiles, workers=WORKERS, recon_fractions=RECON_FRACTIONS, bfs_clusters=BFS_CLUSTERS, reps: int = 1,
-             device: int = 0) -> dict:
-    """Best {"workers", "recon_max_ctas", "bfs_max_cluster", "mpx_s"} over the
-    grid, and every measurement under "trials"."""
+def cache_path() -> str:
+    return os.environ.get("NSG_AUTOTUNE_CACHE") or os.path.join(os.path.expanduser("~"), ".cache", "nsg",
+                                                                 "autotune.json")
+
+
+def cache_key(tiles, device: int = 0) -> str:
+    """GPU name and SM count, and a digest of the batch's tile shapes."""
+    p = torch.cuda.get_device_properties(device)
+    shapes = sorted((int(t.shape[0]), int(t.shape[1])) for t in tiles)
+    mix = hashlib.sha256(json.dumps(shapes).encode()).hexdigest()[:16]
+    return f"{p.name}|{p.multi_processor_count}|{mix}"
+
+
+def _timed(pool, arr, params, reps: int) -> float:
+    """ms per batch: CUDA events around `reps` blocking batch calls."""
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        pool.run(arr, params)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def autotune(tiles, workers=WORKERS, recon_fractions=RECON_FRACTIONS, bfs_clusters=BFS_CLUSTERS,
+             switchover=RECON_SWITCHOVER, reps: int = 3, device: int = 0, use_cache: bool = True) -> dict:
+    """Best {"workers", "recon_max_ctas", "bfs_max_cluster", "recon_wl_phases",
+    "mpx_s"} and every measurement under "trials"."""
+    key = cache_key(tiles, device)
+    path = cache_path()
+    if use_cache and os.path.exists(path):
+        try:
+            with open(path) as f:
+                hit = json.load(f).get(key)
+            if hit:
+                return dict(hit, cached=True)
+        except (OSError, ValueError):
+            pass
     sms = torch.cuda.get_device_properties(device).multi_processor_count
     maxr = max(t.shape[0] for t in tiles)
     maxc = max(t.shape[1] for t in tiles)
@@ -56,24 +101,63 @@ def autotune(tiles, workers=WORKERS, recon_fractions=RECON_FRACTIONS, bfs_cluste
     arr, _labels = _tile_array(tiles)
     params = _lib.SegParams()
     trials = []
+
+    def measure(pool, w, rc, bfs, wl, n):
+        pool.set_tuning(rc, bfs, wl)
+        pool.run(arr, params)  # warm-up
+        ms = _timed(pool, arr, params, n)
+        t = {"workers": w, "recon_max_ctas": rc, "bfs_max_cluster": bfs, "recon_wl_phases": wl,
+             "mpx_s": round(px / ms / 1e3, 2), "reps": n}
+        trials.append(t)
+        return t
+
+    # 1. every (workers, grid, cluster) once, with scans until stable
+    first = []
     for w in workers:
         pool = TilePool(maxr, maxc, workers=w, device=device)
         try:
-            for frac, bfs in itertools.product(recon_fractions, bfs_clusters):
-                rc = max(1, int(sms * frac))
-                pool.set_tuning(rc, bfs)
-                pool.run(arr, params)  # warm-up
-                torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                for _ in range(reps):
-                    pool.run(arr, params)
-                torch.cuda.synchronize()
-                mpx = px * reps / (time.perf_counter() - t0) / 1e6
-                trials.append({"workers": w, "recon_max_ctas": rc, "bfs_max_cluster": bfs, "mpx_s": round(mpx, 2)})
+            for frac in recon_fractions:
+                for bfs in bfs_clusters:
+                    first.append(measure(pool, w, max(1, int(sms * frac)), bfs, 0, 1))
         finally:
             pool.close()
-    best = max(trials, key=lambda t: t["mpx_s"])
-    return dict(best, trials=trials, calibration_tiles=len(tiles), calibration_mpx=round(px / 1e6, 1))
+    # 2. the three best again, `reps` timed repetitions each
+    top = sorted(first, key=lambda t: -t["mpx_s"])[:3]
+    second = []
+    for w in sorted({t["workers"] for t in top}):
+        pool = TilePool(maxr, maxc, workers=w, device=device)
+        try:
+            for t in top:
+                if t["workers"] == w:
+                    second.append(measure(pool, w, t["recon_max_ctas"], t["bfs_max_cluster"], 0, reps))
+        finally:
+            pool.close()
+    best = max(second, key=lambda t: t["mpx_s"])
+    # 3. the scan-to-queue switchover at the best launch shape
+    pool = TilePool(maxr, maxc, workers=best["workers"], device=device)
+    try:
+        for wl in switchover:
+            if wl != 0:
+                t = measure(pool, best["workers"], best["recon_max_ctas"], best["bfs_max_cluster"], wl, reps)
+                if t["mpx_s"] > best["mpx_s"]:
+                    best = t
+    finally:
+        pool.close()
+    res = dict(best, trials=trials, calibration_tiles=len(tiles), calibration_mpx=round(px / 1e6, 1), key=key)
+    if use_cache:
+        try:
+            os.makedirs(os.path.dirname(path), exist_ok=True)
+            data = {}
+            if os.path.exists(path):
+                with open(path) as f:
+                    data = json.load(f)
+            data[key] = res
+            with open(path + ".tmp", "w") as f:
+                json.dump(data, f)
+            os.replace(path + ".tmp", path)
+        except (OSError, ValueError):
+            pass
+    return dict(res, cached=False)
 
 
 def main(argv=None) -> int:
@@ -81,10 +165,11 @@ def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--tiles", type=int, default=96)
     ap.add_argument("--out", default="")
+    ap.add_argument("--no-cache", action="store_true")
     a = ap.parse_args(argv)
-    shapes = synth_torch.batch_shapes(256)[: a.tiles]
-    tiles = [synth_torch.he_tile(r, c, 0x5EED0003 + i, device="cuda") for i, (r, c) in enumerate(shapes)]
-    res = autotune(tiles)
+    shapes = synth_torch.batch_shapes(a.tiles, seed=0x5EEDCA11)
+    tiles = [synth_torch.he_tile(r, c, 0x5EEDCA11 + i, device="cuda") for i, (r, c) in enumerate(shapes)]
+    res = autotune(tiles, use_cache=not a.no_cache)
     text = json.dumps(res, indent=1)
     if a.out:
         with open(a.out, "w") as f:

@@ -11,7 +11,10 @@
 //    counter over the tiles sorted largest first, so that the batch ends on
 //    small tiles;
 //  * nsg_server_*: tiles are submitted one at a time into a bounded FIFO and
-//    results are polled; the number of workers is what a memory budget admits.
+//    results are polled; the number of workers is what a memory budget admits,
+//    either all of one size or split over size classes
+//    (nsg_server_create_classes), so that a small tile holds a small
+//    workspace; a full queue rejects new tiles (the caller sheds or retries).
 //
 // Host code only: the device work is the pipeline of pipeline.cu.
 #include <algorithm>
@@ -35,12 +38,19 @@ struct Job {
     nsg_seg_params prm;
     long long ticket;
     Clock::time_point t_submit;
+    int64_t need;  // capacity (pixels) of the smallest worker class that holds the tile
 };
 
 struct Worker {
     nsg_context *ctx = nullptr;
     cudaStream_t stream = nullptr;
     std::thread th;
+    int max_rows = 0, max_cols = 0;  // the largest tile its context holds
+    bool fits(int rows, int cols) const {
+        return rows > 0 && cols > 0 && (int64_t)rows * cols <= (int64_t)max_rows * max_cols &&
+               (int64_t)(rows + 2) * (cols + 2) <= (int64_t)(max_rows + 2) * (max_cols + 2);
+    }
+    int64_t capacity() const { return (int64_t)max_rows * max_cols; }
 };
 
 // H channel (colour deconvolution with the feature pipeline's stains) and
@@ -141,6 +151,31 @@ struct nsg_pool {
     std::deque<nsg_result> done;
     int qcap = 0;
     long long next_ticket = 0;
+    int64_t smallest_class = 0;  // capacity (pixels) of the smallest worker class
+
+    // the smallest worker class (capacity in pixels) that holds a rows x cols
+    // tile, 0 when none does
+    int64_t class_for(int rows, int cols) const {
+        int64_t best = 0;
+        for (const Worker &o : w)
+            if (o.fits(rows, cols) && (best == 0 || o.capacity() < best)) best = o.capacity();
+        return best;
+    }
+
+    // The server's admission: a worker takes the oldest queued tile of its own
+    // size class first (the tiles that need a context of its size), else the
+    // oldest queued tile that fits its context at all, so that small tiles do
+    // not keep larger ones waiting for the large workers while no worker idles
+    // with work it could do.  -1: nothing fits.
+    int pick_job(const Worker &me) const {
+        int any = -1;
+        const int64_t mine = me.capacity();
+        for (int i = 0; i < (int)q.size(); ++i) {
+            if (q[i].need == mine) return i;
+            if (any < 0 && q[i].need <= mine && me.fits(q[i].tile.rows, q[i].tile.cols)) any = i;
+        }
+        return any;
+    }
 
     void work(int k) {
         cudaSetDevice(device);
@@ -148,11 +183,16 @@ struct nsg_pool {
         unsigned long long seen = 0;
         for (;;) {
             std::unique_lock<std::mutex> lk(mu);
-            cv_work.wait(lk, [&] { return quit || gen != seen || !q.empty(); });
+            int pick = -1;
+            cv_work.wait(lk, [&] {
+                if (quit || gen != seen) return true;
+                pick = pick_job(me);
+                return pick >= 0;
+            });
             if (quit) return;
-            if (gen == seen && !q.empty()) {
-                Job j = q.front();
-                q.pop_front();
+            if (gen == seen && pick >= 0) {
+                Job j = q[pick];
+                q.erase(q.begin() + pick);
                 lk.unlock();
                 run_tile(me.ctx, me.stream, j.tile, j.prm, true);
                 nsg_result r;
@@ -217,8 +257,16 @@ size_t nsg_pool_context_bytes(int max_rows, int max_cols) {
     return nsg::context_bytes_for(max_rows, max_cols);
 }
 
-int nsg_pool_create(nsg_pool **out, int max_rows, int max_cols, int workers, int device) {
-    if (!out || max_rows <= 0 || max_cols <= 0 || workers <= 0 || workers > 256) return NSG_ERR_ARG;
+}  // extern "C"
+
+namespace {
+
+// a pool whose worker k holds tiles up to dims[2k] x dims[2k+1]
+int pool_create_dims(nsg_pool **out, const std::vector<int> &dims, int device) {
+    const int workers = (int)dims.size() / 2;
+    if (!out || workers <= 0 || workers > 256) return NSG_ERR_ARG;
+    for (int v : dims)
+        if (v <= 0) return NSG_ERR_ARG;
     *out = nullptr;
     nsg_pool *p = new (std::nothrow) nsg_pool();
     if (!p) return NSG_ERR_OOM;
@@ -228,8 +276,13 @@ int nsg_pool_create(nsg_pool **out, int max_rows, int max_cols, int workers, int
         delete p;
         return NSG_ERR_CUDA;
     }
-    for (auto &w : p->w) {
-        int r = nsg_context_create(&w.ctx, max_rows, max_cols, device);
+    p->smallest_class = 0;
+    for (int k = 0; k < workers; ++k) {
+        Worker &w = p->w[k];
+        w.max_rows = dims[2 * k];
+        w.max_cols = dims[2 * k + 1];
+        if (p->smallest_class == 0 || w.capacity() < p->smallest_class) p->smallest_class = w.capacity();
+        int r = nsg_context_create(&w.ctx, w.max_rows, w.max_cols, device);
         if (r == NSG_SUCCESS && cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking) != cudaSuccess)
             r = NSG_ERR_CUDA;
         if (r != NSG_SUCCESS) {
@@ -252,6 +305,17 @@ int nsg_pool_create(nsg_pool **out, int max_rows, int max_cols, int workers, int
     for (int k = 0; k < workers; ++k) p->w[k].th = std::thread([p, k] { p->work(k); });
     *out = p;
     return NSG_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nsg_pool_create(nsg_pool **out, int max_rows, int max_cols, int workers, int device) {
+    if (!out || max_rows <= 0 || max_cols <= 0 || workers <= 0 || workers > 256) return NSG_ERR_ARG;
+    std::vector<int> dims;
+    for (int k = 0; k < workers; ++k) dims.push_back(max_rows), dims.push_back(max_cols);
+    return pool_create_dims(out, dims, device);
 }
 
 int nsg_pool_destroy(nsg_pool *p) {
@@ -348,16 +412,93 @@ int nsg_server_create(nsg_server **out, int max_rows, int max_cols, size_t budge
     return NSG_SUCCESS;
 }
 
+int nsg_server_create_classes(nsg_server **out, const int *class_rows, const int *class_cols, const double *weights,
+                              int nclasses, size_t budget, int queue_cap, int device) {
+    if (!out || !class_rows || !class_cols || nclasses <= 0 || nclasses > 16 || queue_cap <= 0) return NSG_ERR_ARG;
+    *out = nullptr;
+    // workers per class: budget split in proportion to weight x bytes, i.e.
+    // c_k = floor(lambda * w_k) with lambda = budget / sum(w_j * bytes_j);
+    // the largest class keeps at least one worker so that every tile that fits
+    // some class can be served
+    std::vector<size_t> bytes(nclasses);
+    double wsum = 0.0;
+    int largest = 0;
+    for (int k = 0; k < nclasses; ++k) {
+        bytes[k] = nsg_pool_context_bytes(class_rows[k], class_cols[k]);
+        const double wk = weights ? weights[k] : 1.0;
+        if (bytes[k] == 0 || !(wk >= 0.0)) return NSG_ERR_ARG;
+        wsum += wk * (double)bytes[k];
+        if ((int64_t)class_rows[k] * class_cols[k] > (int64_t)class_rows[largest] * class_cols[largest]) largest = k;
+    }
+    if (bytes[largest] > budget) return NSG_ERR_OOM;  // not even one context of the largest class
+    std::vector<int> count(nclasses, 0);
+    size_t used = 0;
+    int total = 0;
+    if (wsum > 0.0) {
+        const double lambda = (double)budget / wsum;
+        for (int k = 0; k < nclasses; ++k) {
+            count[k] = (int)((weights ? weights[k] : 1.0) * lambda);
+            used += (size_t)count[k] * bytes[k];
+            total += count[k];
+        }
+    }
+    if (count[largest] == 0) {
+        // make room for one large worker by dropping small ones, smallest first
+        while (used + bytes[largest] > budget) {
+            int victim = -1;
+            for (int k = 0; k < nclasses; ++k)
+                if (count[k] > 0 && (victim < 0 || bytes[k] < bytes[victim])) victim = k;
+            if (victim < 0) break;
+            --count[victim];
+            used -= bytes[victim];
+            --total;
+        }
+        count[largest] = 1;
+        ++total;
+    }
+    // at most 64 workers (64 streams already share the 32 hardware queues)
+    while (total > 64) {
+        int k = 0;
+        for (int j = 1; j < nclasses; ++j)
+            if (count[j] > count[k]) k = j;
+        --count[k];
+        --total;
+    }
+    std::vector<int> dims;
+    for (int k = 0; k < nclasses; ++k)
+        for (int i = 0; i < count[k]; ++i) dims.push_back(class_rows[k]), dims.push_back(class_cols[k]);
+    nsg_server *srv = new (std::nothrow) nsg_server();
+    if (!srv) return NSG_ERR_OOM;
+    const int r = pool_create_dims(&srv->pool, dims, device);
+    if (r != NSG_SUCCESS) {
+        delete srv;
+        return r;
+    }
+    srv->pool->qcap = queue_cap;
+    *out = srv;
+    return NSG_SUCCESS;
+}
+
 int nsg_server_workers(const nsg_server *s) { return s ? nsg_pool_workers(s->pool) : 0; }
+
+int nsg_server_class_workers(const nsg_server *s, int max_rows, int max_cols) {
+    if (!s) return NSG_ERR_ARG;
+    int n = 0;
+    for (const Worker &w : s->pool->w) n += w.max_rows == max_rows && w.max_cols == max_cols;
+    return n;
+}
 
 int nsg_server_submit(nsg_server *s, const nsg_tile *tile, const nsg_seg_params *prm, long long *ticket) {
     if (!s || !tile || !tile->bgr) return NSG_ERR_ARG;
     nsg_pool *p = s->pool;
+    const int64_t need = p->class_for(tile->rows, tile->cols);
+    if (need == 0) return tile->rows > 0 && tile->cols > 0 ? NSG_ERR_OOM : NSG_ERR_ARG;  // no class holds it
     Job j;
     j.tile = *tile;
     if (prm) j.prm = *prm;
     else nsg_default_params(&j.prm);
     j.t_submit = Clock::now();
+    j.need = need;
     {
         std::lock_guard<std::mutex> lk(p->mu);
         if ((int)p->q.size() >= p->qcap) return NSG_ERR_QUEUE_FULL;
@@ -365,7 +506,7 @@ int nsg_server_submit(nsg_server *s, const nsg_tile *tile, const nsg_seg_params 
         p->q.push_back(j);
     }
     if (ticket) *ticket = j.ticket;
-    p->cv_work.notify_one();
+    p->cv_work.notify_all();  // only a worker whose class holds the tile can take it
     return NSG_SUCCESS;
 }
 

@@ -179,9 +179,12 @@ int nsg_context_destroy(nsg_context *h) {
 const char *nsg_context_last_error(const nsg_context *h) { return h ? h->c.last_error.c_str() : "null context"; }
 
 int nsg_context_set_tuning(nsg_context *h, const nsg_tuning *t) {
-    if (!h || !t || t->recon_max_ctas < 0 || t->bfs_max_cluster < 0 || t->bfs_max_cluster > 16) return NSG_ERR_ARG;
+    if (!h || !t || t->recon_max_ctas < 0 || t->bfs_max_cluster < 0 || t->bfs_max_cluster > 16 ||
+        t->recon_wl_phases < -1 || t->recon_wl_phases > 8)
+        return NSG_ERR_ARG;
     h->c.recon_max_ctas = t->recon_max_ctas;
     h->c.bfs_max_cluster = t->bfs_max_cluster;
+    h->c.recon_wl_phases = t->recon_wl_phases;
     return NSG_SUCCESS;
 }
 

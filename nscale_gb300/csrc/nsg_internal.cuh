@@ -96,6 +96,7 @@ struct Ctx {
     cudaEvent_t ev_counts = nullptr;  // marks a posted readback of the device counters
     int recon_max_ctas = 0;           // cap on the reconstruction's persistent grid (0: one CTA per SM)
     int bfs_max_cluster = 0;          // largest BFS thread-block cluster tried (0: 16)
+    int recon_wl_phases = -1;         // scan-to-queue switchover of the reconstruction (-1: default)
     std::string last_error;
 };
 

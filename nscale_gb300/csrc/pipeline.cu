@@ -5,7 +5,10 @@
 // (plFindNucleusCandidates :115-304, plSeparateNuclei :308-449).  All
 // intermediates live in the context's arena; the host only reads back the
 // three counts the reference branches on (background ratio, components after
-// the first and the last area filter) and the final component count.
+// the first and the last area filter) and the final component count.  The
+// background ratio is read right after the front passes, as the reference
+// decides it first; the other two are posted and read only where the branch
+// is taken, so the stream keeps running meanwhile.
 #include <float.h>
 #include <limits.h>
 #include <string.h>
@@ -158,7 +161,16 @@ int segment_nuclei_dev(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int
     NSG_TRY(background_count(c, bgr, stride, rows, cols, p.blue, p.green, p.red, nullptr, c.ws.ctr64, s));
     NSG_TRY(front_rbc(c, bgr, stride, rows, cols, p.T1, p.T2, P[0], P[1], P[2], P[3], ctrl + C_COUNT0, s));
     t_mark(c, 0, s);
-    NSG_TRY(post_counts(c, s));  // background ratio, decided after the reconstruction is enqueued
+    // the background ratio decides before anything expensive runs (HE:123-137):
+    // the readback waits only for the two front passes, and a tissue-free tile
+    // costs no reconstruction
+    NSG_TRY(post_counts(c, s));
+    NSG_TRY(take_counts(c));
+    {
+        float ratio = (float)c.ws.h_ctr64[0] / (float)n;  // HE:125-126
+        if (ratio >= 0.99) return fail_fill(NSG_BACKGROUND);
+        if (ratio >= 0.9) return fail_fill(NSG_BACKGROUND_LIKELY);
+    }
     // rbc = bwselect(bw2, bw1, 8) & imR2B (no seeds -> all zero, HE:73-79)
     NSG_TRY(bwselect_dev(c, P[2], P[1], P[4], rows, cols, 8, s));
     and_u8<<<g, kB, 0, s>>>(P[4], P[3], n);
@@ -176,12 +188,6 @@ int segment_nuclei_dev(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int
     // diffIm > G1, diffIm > G2
     NSG_TRY(diff_threshold(c, P[0], P[7], rows, cols, p.G1, p.G2, P[5], P[8], s));
     t_mark(c, 3, s);
-    NSG_TRY(take_counts(c));
-    {
-        float ratio = (float)c.ws.h_ctr64[0] / (float)n;  // HE:125-126
-        if (ratio >= 0.99) return fail_fill(NSG_BACKGROUND);
-        if (ratio >= 0.9) return fail_fill(NSG_BACKGROUND_LIKELY);
-    }
     // bw1 = imfillHoles(diffIm > G1, fillHolesConnectivity)
     NSG_TRY(fill_holes_dev(c, P[5], P[6], rows, cols, p.fillHolesConnectivity, s));
     t_mark(c, 4, s);

@@ -273,6 +273,7 @@ struct Queue {
     long long budget;
     int idle_limit;  // empty-queue polls before an idle CTA leaves (0: stay until done)
     int seq_min;     // dirty lines of a 32-line group from which lanes scan one line each
+    int wl_phases;   // row + column phase pairs a whole-tile pass runs before the pixel worklist
 };
 
 // lane 0 only
@@ -359,6 +360,30 @@ struct TileSmem {
     T mN[TW + 2], mS[TW + 2], mW[TH], mE[TH];  // the mask just outside the tile (neighbours' pixels)
     unsigned drow[TH / 32], dcol[TW / 32];     // dirty rows / columns
     int edges, tile, again, sweeps, dirty, lines;
+};
+
+// The same tile plus the in-tile pixel worklist (see wl_run): a ring of
+// tile-local pixel indices, the set of queued pixels, and the pixels the last
+// column phase changed (column-major bits), which seed the worklist.
+//
+// The ring is a bounded multi-producer / multi-consumer queue with a sequence
+// number per slot (the slot of ticket t is t mod kCap): a producer with
+// ticket t writes only once the slot's sequence is t, and publishes t + 1; a
+// consumer with ticket t reads only once the sequence is t + 1, and frees
+// the slot for ticket t + kCap.  A slot word holds the sequence (mod 2^SB) in
+// its high bits and the pixel index in its low VB bits.  Tickets count up
+// for the CTA's lifetime; since a pixel is queued at most once at a time,
+// at most kCap tickets are outstanding, so producers never wait for space.
+template <typename T, int TW, int TH, int P>
+struct TileWL : TileSmem<T, TW, TH, P> {
+    static constexpr int kCap = TW * TH;  // every pixel at most once in the ring
+    static constexpr int VB = kCap == 16384 ? 14 : (kCap == 4096 ? 12 : 0);
+    static_assert(VB > 0, "tile of 128 x 128 or 64 x 64 pixels");
+    static constexpr unsigned kSeqMask = (1u << (32 - VB)) - 1u;
+    unsigned ring[kCap];
+    unsigned inq[TW * TH / 32];  // row-major pixel bits
+    unsigned cbm[TW * TH / 32];  // column-major: bit c * TH + r
+    int head, tail, pending, abort, raised;
 };
 
 // Whole warp: lane l changed the pixels of its K-pixel slice (l*K .. l*K+K-1)
@@ -571,14 +596,214 @@ __device__ __forceinline__ void mark_dirty_seq(unsigned *m, const unsigned (&chg
     }
 }
 
+
+// ---- in-tile pixel worklist --------------------------------------------------
+// After one row + column phase pair, what is left to propagate inside a tile
+// follows winding single-pixel paths (noisy masks), where further phase
+// pairs rescan whole lines for a one-pixel advance.  The rest is therefore
+// run as an asynchronous worklist in shared memory: a popped pixel p raises
+// every in-tile neighbour q with o[q] < min(o[p], m[q]) to that value and
+// queues q unless it is queued already.  Values only grow and every raise
+// re-queues, so the worklist ends at the same least fixed point as the scans
+// (the result does not depend on the order).  Warps claim up to 32 ring slots
+// at a time; `pending` (queued + in progress) reaching 0 ends the tile.  All
+// waits are bounded by the spin budget; running out sets DEV_TIMEOUT.
+
+// raise o[idx] to `cand` if it is below; true when this call raised it
+__device__ __forceinline__ bool wl_raise(uint8_t *o, int idx, uint8_t cand) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(o + idx);
+    unsigned *w = reinterpret_cast<unsigned *>(a & ~(uintptr_t)3);
+    const int sh = (int)(a & 3) * 8;
+    unsigned old = *reinterpret_cast<volatile unsigned *>(w);
+    for (int guard = 0; guard < 4096; ++guard) {
+        if (((old >> sh) & 255u) >= cand) return false;
+        const unsigned nw = (old & ~(255u << sh)) | ((unsigned)cand << sh);
+        const unsigned prev = atomicCAS(w, old, nw);
+        if (prev == old) return true;
+        old = prev;
+    }
+    return false;  // unreachable: each failed exchange saw a larger value
+}
+__device__ __forceinline__ bool wl_raise(float *o, int idx, float cand) {
+    int *w = reinterpret_cast<int *>(o + idx);
+    int old = *reinterpret_cast<volatile int *>(w);
+    for (int guard = 0; guard < (1 << 20); ++guard) {
+        if (!(__int_as_float(old) < cand)) return false;
+        const int prev = atomicCAS(w, old, __float_as_int(cand));
+        if (prev == old) return true;
+        old = prev;
+    }
+    return false;
+}
+
+template <typename T>
+__device__ __forceinline__ T vld(const T *p) {
+    return *reinterpret_cast<const volatile T *>(p);
+}
+
+// queue pixel p (tile-local index r * TW + c) if it is not queued already
+template <typename WLT>
+__device__ __forceinline__ void wl_push(WLT &sm, int p, long long budget, int *status) {
+    const unsigned bit = 1u << (p & 31);
+    if (atomicOr(&sm.inq[p >> 5], bit) & bit) return;
+    atomicAdd(&sm.pending, 1);
+    const unsigned t = (unsigned)atomicAdd(&sm.tail, 1);
+    volatile unsigned *slot = &sm.ring[t & (WLT::kCap - 1)];
+    for (long long k = 0; (*slot >> WLT::VB) != (t & WLT::kSeqMask); ++k) {
+        if (k > budget) {  // cannot happen while at most kCap tickets are outstanding
+            atomicOr(status, DEV_TIMEOUT);
+            atomicExch(&sm.abort, 1);
+            return;
+        }
+    }
+    *slot = (((t + 1u) & WLT::kSeqMask) << WLT::VB) | (unsigned)p;
+}
+
+// every thread of the CTA; returns when the worklist is empty (or aborted)
+template <typename T, int TW, int TH, int P, int NW>
+__device__ void wl_run(TileWL<T, TW, TH, P> &sm, bool conn8, long long budget, int *status) {
+    using W = TileWL<T, TW, TH, P>;
+    static_assert((W::kCap & (W::kCap - 1)) == 0, "ring capacity must be a power of two");
+    const int lane = threadIdx.x & 31;
+    T *o = sm.o;
+    long long spins = 0;
+    for (;;) {
+        if (vld(&sm.abort)) break;
+        int h = 0, n = 0;
+        if (lane == 0) {
+            const int hh = vld(&sm.head), tt = vld(&sm.tail);
+            if (hh < tt) {
+                const int want = tt - hh < 32 ? tt - hh : 32;
+                if (atomicCAS(&sm.head, hh, hh + want) == hh) h = hh, n = want;
+            } else if (vld(&sm.pending) == 0) {
+                n = -1;
+            }
+        }
+        n = __shfl_sync(0xffffffffu, n, 0);
+        h = __shfl_sync(0xffffffffu, h, 0);
+        if (n < 0) break;
+        if (n == 0) {
+            if (++spins > budget) {
+                if (lane == 0) {
+                    atomicOr(status, DEV_TIMEOUT);
+                    atomicExch(&sm.abort, 1);
+                }
+                break;
+            }
+            continue;
+        }
+        if (lane < n) {
+            const unsigned t = (unsigned)(h + lane);
+            volatile unsigned *slot = &sm.ring[t & (W::kCap - 1)];
+            unsigned word = *slot;
+            bool ok = true;
+            for (long long k = 0; (word >> W::VB) != ((t + 1u) & W::kSeqMask); word = *slot, ++k) {
+                if (k > budget) {
+                    atomicOr(status, DEV_TIMEOUT);
+                    atomicExch(&sm.abort, 1);
+                    ok = false;
+                    break;
+                }
+            }
+            if (ok) {
+                const int p = (int)(word & ((1u << W::VB) - 1u));
+                *slot = ((t + (unsigned)W::kCap) & W::kSeqMask) << W::VB;  // free for ticket t + kCap
+                atomicAnd(&sm.inq[p >> 5], ~(1u << (p & 31)));
+                __threadfence_block();
+                const int r = p / TW, c = p - r * TW;
+                const T v = vld(&o[(r + 1) * P + c + 1]);
+                bool any = false;
+#pragma unroll
+                for (int d = 0; d < 8; ++d) {
+                    const int dy = d < 3 ? -1 : (d < 5 ? 0 : 1);
+                    const int dx = d < 3 ? d - 1 : (d < 5 ? (d == 3 ? -1 : 1) : d - 6);
+                    if (!conn8 && dy != 0 && dx != 0) continue;
+                    const int rq = r + dy, cq = c + dx;
+                    if (rq < 0 || rq >= TH || cq < 0 || cq >= TW) continue;
+                    const T mq = sm.m[rq * P + cq];
+                    const T cand = smin(v, mq);
+                    const int oi = (rq + 1) * P + cq + 1;
+                    if (vld(&o[oi]) < cand && wl_raise(o, oi, cand)) {
+                        any = true;
+                        wl_push(sm, rq * TW + cq, budget, status);
+                    }
+                }
+                if (any) sm.raised = 1;
+                atomicSub(&sm.pending, 1);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Seed the worklist from the pixels the last column phase changed (cbm),
+// then clear cbm.  Called by every thread; ends with a barrier.
+template <typename T, int TW, int TH, int P, int NW>
+__device__ void wl_seed_changed(TileWL<T, TW, TH, P> &sm, long long budget, int *status) {
+    constexpr int NWORD = TW * TH / 32;
+    for (int w = threadIdx.x; w < NWORD; w += NW * 32) {
+        unsigned b = sm.cbm[w];
+        sm.cbm[w] = 0;
+        while (b) {
+            const int k = __ffs(b) - 1;
+            b &= b - 1;
+            const int bit = w * 32 + k;  // column-major: c * TH + r
+            const int c = bit / TH, r = bit - c * TH;
+            wl_push(sm, r * TW + c, budget, status);
+        }
+    }
+    __syncthreads();
+}
+
+// Seed from the halo on the sides in `dirty_in`: an edge pixel below
+// min(halo neighbour, its mask) is raised to it and queued.  The worklist
+// then carries the change inward.  Ends with a barrier.
+template <typename T, int TW, int TH, int P, int NW>
+__device__ void wl_seed_halo(TileWL<T, TW, TH, P> &sm, int dirty_in, bool conn8, long long budget, int *status) {
+    T *o = sm.o;
+    const int c8 = conn8 ? 1 : 0;
+    auto pull = [&](int r, int c, int hr, int hc0, int hstep) {
+        // pixel (r, c) from the halo pixels hr/hc0 + k * hstep, k = -c8..c8
+        const T mq = sm.m[r * P + c];
+        T best = (T)0;
+        bool have = false;
+        for (int k = -c8; k <= c8; ++k) {
+            const int yy = hr + (hstep ? 0 : k), xx = hc0 + (hstep ? k : 0);
+            const T hv = vld(&o[(yy + 1) * P + xx + 1]);
+            const T cand = smin(hv, mq);
+            if (!have || best < cand) best = cand, have = true;
+        }
+        const int oi = (r + 1) * P + c + 1;
+        if (vld(&o[oi]) < best && wl_raise(o, oi, best)) {
+            sm.raised = 1;
+            wl_push(sm, r * TW + c, budget, status);
+        }
+    };
+    if (dirty_in & D_N)
+        for (int c = threadIdx.x; c < TW; c += NW * 32) pull(0, c, -1, c, 1);
+    if (dirty_in & D_S)
+        for (int c = threadIdx.x; c < TW; c += NW * 32) pull(TH - 1, c, TH, c, 1);
+    if (dirty_in & D_W)
+        for (int r = threadIdx.x; r < TH; r += NW * 32) pull(r, 0, r, -1, 0);
+    if (dirty_in & D_E)
+        for (int r = threadIdx.x; r < TH; r += NW * 32) pull(r, TW - 1, r, TW, 0);
+    __syncthreads();
+}
+
 // One pass over tile (tx, ty): load, alternate row / column phases over the
 // dirty lines until nothing changes, report which neighbours must run again,
 // write back.
-template <typename T, int TW, int TH, int P, int NW, bool HYB = false>
+//
+// WL: a pass over a whole tile (D_ALL / D_FRESH) runs `wl_phases` row +
+// column phase pairs and hands what is still moving to the pixel worklist
+// (seeded with the pixels the last column phase changed); a pass for changed
+// halo sides skips the phases and seeds the worklist from those sides.
+template <typename T, int TW, int TH, int P, int NW, bool HYB, bool WL, typename SM>
 __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, int cols, bool conn8, int tx, int ty,
-                                 int dirty_in, TileSmem<T, TW, TH, P> &sm, int seq_min = kSeqMinLines) {
+                                 int dirty_in, SM &sm, int seq_min, int wl_phases, long long budget, int *status) {
     static_assert(!HYB || (std::is_same<T, uint8_t>::value && NW == TH / 32 && NW == TW / 32),
                   "lane-per-line scans: uint8, one warp per 32-line group");
+    constexpr int NWORD = TW * TH / 32;
     constexpr int KX = TW / 32, KY = TH / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int y0 = ty * TH, x0 = tx * TW;
@@ -624,6 +849,11 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
         sm.edges = 0;
         sm.sweeps = 0;
         sm.lines = 0;
+        if constexpr (WL) {
+            sm.pending = 0;
+            sm.abort = 0;
+            sm.raised = 0;
+        }
     }
     __syncthreads();
     for (int i = threadIdx.x; i < TW; i += NW * 32) {
@@ -637,7 +867,12 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
     unsigned my_edges = 0;
     bool anych = false;
     const int vr = rows - y0, vc = cols - x0;  // valid extent of this tile
-    for (int it = 0; it < 1024; ++it) {
+    const bool phases = !WL || (dirty_in & (D_ALL | D_FRESH));
+    const int max_it = WL ? wl_phases : 1024;
+    bool need_wl = false;
+    for (int it = 0; phases && it < max_it; ++it) {
+        if constexpr (WL)
+            for (int w = threadIdx.x; w < NWORD; w += NW * 32) sm.cbm[w] = 0;
         // ---- row phase over the dirty rows (round robin over warps)
         unsigned rm[TH / 32];
 #pragma unroll
@@ -721,6 +956,11 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
                     if (warp == w) {
                         unsigned chg[TH / 32] = {};
                         if ((bits >> lane) & 1u) col_seq<TH, P>(o, sm.m, w * 32 + lane, conn8, chg);
+                        if constexpr (WL) {
+#pragma unroll
+                            for (int j = 0; j < TH / 32; ++j)
+                                if (chg[j]) sm.cbm[(w * 32 + lane) * (TH / 32) + j] = chg[j];
+                        }
                         unsigned any = 0;
 #pragma unroll
                         for (int j = 0; j < TH / 32; ++j) any |= chg[j];
@@ -759,6 +999,10 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
                         changed |= 1u << k;
                     }
                 }
+                if constexpr (WL) {
+                    if (changed)
+                        atomicOr(&sm.cbm[cidx * (TH / 32) + ((lane * KY) >> 5)], changed << ((lane * KY) & 31));
+                }
                 if (__any_sync(0xffffffffu, changed != 0)) {
                     chc = true;
                     mark_dirty<KY, TH>(sm.drow, changed);
@@ -769,7 +1013,19 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
         if (threadIdx.x == 0) sm.sweeps = it + 1;
         anych = anych || chr || chc;
         if (!chc) break;  // no row is dirty: the tile is stable
-        if (it == 1023) my_edges |= 16u;  // not stable yet: process again later
+        if (it == max_it - 1) {
+            if (WL) need_wl = true;  // the worklist finishes the tile
+            else my_edges |= 16u;    // not stable yet: process again later
+        }
+    }
+    if constexpr (WL) {
+        if (need_wl) wl_seed_changed<T, TW, TH, P, NW>(sm, budget, status);
+        else if (!phases) wl_seed_halo<T, TW, TH, P, NW>(sm, dirty_in, conn8, budget, status);
+        if (need_wl || !phases) {
+            wl_run<T, TW, TH, P, NW>(sm, conn8, budget, status);
+            __syncthreads();
+            if (sm.raised) anych = true;
+        }
     }
     // A neighbour tile needs another pass only if an edge pixel that changed
     // here can raise one of its pixels: new value above that pixel's value
@@ -1144,19 +1400,29 @@ __device__ __forceinline__ void notify(Queue &q, int t, int bits) {
     q_push(q, t);
 }
 
-template <typename T, int TW, int TH, int P, int NW, bool PACKED>
-using TileOf = typename std::conditional<PACKED, TileU8<TW, TH>, TileSmem<T, TW, TH, P>>::type;
+template <typename T, int TW, int TH, int P, int NW, bool PACKED, bool WL = false>
+using TileOf = typename std::conditional<
+    PACKED, TileU8<TW, TH>,
+    typename std::conditional<WL, TileWL<T, TW, TH, P>, TileSmem<T, TW, TH, P>>::type>::type;
 
 // MINB: CTAs per SM the register budget is sized for (8 warps: 4, i.e. at
 // most 64 registers a thread, so the reconstructions of several tiles in
 // flight can share an SM; 2 is kept as a tuning knob)
-template <typename T, int TW, int TH, int P, int NW, bool PACKED, int MINB, bool HYB>
+template <typename T, int TW, int TH, int P, int NW, bool PACKED, int MINB, bool HYB, bool WL>
 __global__ void __launch_bounds__(NW * 32, MINB) recon_cta(const T *__restrict__ mask, T *out, int rows, int cols,
                                                            int conn, int tiles_x, int tiles_y, Queue q) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
-    using Sm = TileOf<T, TW, TH, P, NW, PACKED>;
+    using Sm = TileOf<T, TW, TH, P, NW, PACKED, WL>;
     Sm &sm = *reinterpret_cast<Sm *>(sm_raw);
     const bool conn8 = conn == 8;
+    if constexpr (WL) {
+        // the worklist starts empty (slot i free for ticket i) with nothing
+        // queued; every tile pass leaves it empty
+        for (int i = threadIdx.x; i < Sm::kCap; i += NW * 32) sm.ring[i] = ((unsigned)i & Sm::kSeqMask) << Sm::VB;
+        for (int i = threadIdx.x; i < TW * TH / 32; i += NW * 32) sm.inq[i] = sm.cbm[i] = 0;
+        if (threadIdx.x == 0) sm.head = sm.tail = 0;
+        __syncthreads();
+    }
     for (;;) {
         if (threadIdx.x == 0) sm.tile = q_pop(q);
         __syncthreads();
@@ -1172,7 +1438,13 @@ __global__ void __launch_bounds__(NW * 32, MINB) recon_cta(const T *__restrict__
             if constexpr (PACKED)
                 cta_process_tile_u8<TW, TH, NW>(mask, out, rows, cols, conn8, tx, ty, dirty, sm);
             else
-                cta_process_tile<T, TW, TH, P, NW, HYB>(mask, out, rows, cols, conn8, tx, ty, dirty, sm, q.seq_min);
+                cta_process_tile<T, TW, TH, P, NW, HYB, WL>(mask, out, rows, cols, conn8, tx, ty, dirty, sm, q.seq_min,
+                                                            q.wl_phases, q.budget, q.status);
+            if constexpr (WL) {
+                // a worklist wait ran out of budget (DEV_TIMEOUT is set): leave;
+                // the other CTAs see the status word and leave too
+                if (vld(&sm.abort)) return;
+            }
             if (threadIdx.x == 0) {
                 const unsigned edges = (unsigned)sm.edges;
                 // our top edge is the upper tile's bottom halo, and so on
@@ -1200,7 +1472,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) recon_cta(const T *__restrict__
 }
 
 template <typename T, int TW, int TH, int P, int NW, bool PACKED = false, int MINB = (NW >= 16 && !PACKED) ? 1 : 2,
-          bool HYB = false>
+          bool HYB = false, bool WL = false>
 int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int cols, int conn, cudaStream_t s) {
     NSG_TRY(check_dims(c, rows, cols));
     NSG_TRY(check_conn(c, conn));
@@ -1262,9 +1534,14 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
     if (const char *e = getenv("NSG_RECON_IDLE")) q.idle_limit = atoi(e);  // tuning knob
     q.seq_min = kSeqMinLines;
     if (const char *e = getenv("NSG_RECON_SEQMIN")) q.seq_min = atoi(e);  // tuning knob
+    q.wl_phases = c.recon_wl_phases >= 1 ? c.recon_wl_phases : 1;
+    if (const char *e = getenv("NSG_RECON_WLPH")) {  // tuning knob: phase pairs before the worklist (1-8)
+        const int v = atoi(e);
+        if (v >= 1 && v <= 8) q.wl_phases = v;
+    }
     q.stats = c.ws.ctrl + C_RSTATS;
-    const size_t smem = sizeof(TileOf<T, TW, TH, P, NW, PACKED>);
-    auto kfn = recon_cta<T, TW, TH, P, NW, PACKED, MINB, HYB>;
+    const size_t smem = sizeof(TileOf<T, TW, TH, P, NW, PACKED, WL>);
+    auto kfn = recon_cta<T, TW, TH, P, NW, PACKED, MINB, HYB, WL>;
     NSG_CUDA_TRY(c, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     NSG_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, NW * 32, smem));
@@ -1301,6 +1578,17 @@ int recon_warps() {
     return 8;  // more warps shorten one reconstruction but crowd out concurrent tiles
 }
 
+// Tuning knob NSG_RECON_WL=1: the in-tile pixel worklist after NSG_RECON_WLPH
+// phase pairs.  Off by default: measured on GB300, one 4096^2 pipeline
+// reconstruction 9.6 ms (phases until stable) vs 10.6 / 9.5 / 8.8 ms (worklist
+// after 1 / 2 / 3 phase pairs), but the batched form 1018 vs 822 / 868 Mpixel/s
+// (1 / 3 phase pairs): the worklist's serial chains hold a CTA (and its larger
+// shared-memory footprint) longer than the phase loop does.
+bool recon_worklist(const Ctx &c) {
+    if (const char *e = getenv("NSG_RECON_WL")) return atoi(e) != 0;
+    return c.recon_wl_phases >= 1;  // the context's tuning (nsg_tuning.recon_wl_phases)
+}
+
 // register budget of the 8-warp tile CTA: sized for 4 CTAs per SM (default) or 2
 int recon_minb() {
     if (const char *e = getenv("NSG_RECON_MINB")) {  // tuning knob: 2 or 4
@@ -1322,8 +1610,12 @@ int recon_u8(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t *out, i
     }
     bool hyb = true;  // lane-per-line scans for dense line groups, 4 warps (tuning knob NSG_RECON_HYB=0: shuffle scans only)
     if (const char *e = getenv("NSG_RECON_HYB")) hyb = atoi(e) != 0;
-    if (hyb && !getenv("NSG_RECON_WARPS"))
+    if (hyb && !getenv("NSG_RECON_WARPS")) {
+        if (recon_worklist(c))
+            return run_recon_cta<uint8_t, 128, 128, 132, 4, false, 4, true, true>(c, marker, mask, out, rows, cols,
+                                                                                  conn, s);
         return run_recon_cta<uint8_t, 128, 128, 132, 4, false, 4, true>(c, marker, mask, out, rows, cols, conn, s);
+    }
     if (nw == 8) {
         if (recon_minb() == 2) return run_recon_cta<uint8_t, 128, 128, 132, 8, false, 2>(c, marker, mask, out, rows, cols, conn, s);
         return run_recon_cta<uint8_t, 128, 128, 132, 8, false, 4>(c, marker, mask, out, rows, cols, conn, s);
@@ -1336,6 +1628,9 @@ int recon_f32(Ctx &c, const float *marker, const float *mask, float *out, int ro
               cudaStream_t s) {
     const int nw = recon_warps();
     if (nw == 8) {
+        if (recon_worklist(c) && !getenv("NSG_RECON_WARPS"))
+            return run_recon_cta<float, 64, 64, 67, 8, false, 4, false, true>(c, marker, mask, out, rows, cols, conn,
+                                                                              s);
         if (recon_minb() == 2) return run_recon_cta<float, 64, 64, 67, 8, false, 2>(c, marker, mask, out, rows, cols, conn, s);
         return run_recon_cta<float, 64, 64, 67, 8, false, 4>(c, marker, mask, out, rows, cols, conn, s);
     }

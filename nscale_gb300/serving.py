@@ -54,9 +54,10 @@ class TilePool:
     def workers(self) -> int:
         return self.L.nsg_pool_workers(self.h)
 
-    def set_tuning(self, recon_max_ctas: int = 0, bfs_max_cluster: int = 0) -> None:
-        """nsg_pool_set_tuning: launch shapes of every worker (results do not change)."""
-        t = _lib.Tuning(recon_max_ctas, bfs_max_cluster)
+    def set_tuning(self, recon_max_ctas: int = 0, bfs_max_cluster: int = 0, recon_wl_phases: int = -1) -> None:
+        """nsg_pool_set_tuning: launch shapes of every worker and the
+        reconstruction's scan-to-queue switchover (results do not change)."""
+        t = _lib.Tuning(recon_max_ctas, bfs_max_cluster, recon_wl_phases)
         _check(self.L.nsg_pool_set_tuning(self.h, C.byref(t)), "nsg_pool_set_tuning")
 
     def set_timing(self, on: bool = True) -> None:
@@ -130,12 +131,28 @@ class TileServer:
     (at most 64); submit raises NSG_ERR_QUEUE_FULL when `queue_cap` tiles wait."""
 
     def __init__(self, max_rows: int, max_cols: int, memory_budget_bytes: int, queue_cap: int = 64,
-                 device: int = 0):
+                 device: int = 0, classes: list[tuple[int, int]] | None = None,
+                 weights: list[float] | None = None):
+        """classes: [(rows, cols), ...] size classes of the workers' contexts
+        (nsg_server_create_classes: the budget is split in proportion to
+        weight x context bytes); None = every worker max_rows x max_cols."""
         self.L = _lib.load()
         self.h = C.c_void_p()
-        _check(self.L.nsg_server_create(C.byref(self.h), max_rows, max_cols, memory_budget_bytes, queue_cap, device),
-               "nsg_server_create")
+        if classes:
+            n = len(classes)
+            rows = (C.c_int * n)(*[r for r, _ in classes])
+            cols = (C.c_int * n)(*[c for _, c in classes])
+            w = (C.c_double * n)(*(weights or [1.0] * n))
+            _check(self.L.nsg_server_create_classes(C.byref(self.h), rows, cols, w, n, memory_budget_bytes,
+                                                    queue_cap, device), "nsg_server_create_classes")
+        else:
+            _check(self.L.nsg_server_create(C.byref(self.h), max_rows, max_cols, memory_budget_bytes, queue_cap,
+                                            device), "nsg_server_create")
+        self.classes = list(classes) if classes else [(max_rows, max_cols)]
         self._live = {}
+
+    def class_workers(self) -> dict[tuple[int, int], int]:
+        return {c: self.L.nsg_server_class_workers(self.h, c[0], c[1]) for c in self.classes}
 
     @property
     def workers(self) -> int:
@@ -152,7 +169,7 @@ class TileServer:
         t.mask, t.want_bbox, t.want_features = None, 1 if want_bbox else 0, 1 if want_features else 0
         ticket = C.c_longlong(-1)
         _check(self.L.nsg_server_submit(self.h, C.byref(t), C.byref(params) if params else None, C.byref(ticket)),
-               "nsg_server_submit")
+               "nsg_server_submit")  # NSG_ERR_QUEUE_FULL when queue_cap tiles wait: the caller sheds
         self._live[ticket.value] = (image, labels)
         return ticket.value
 

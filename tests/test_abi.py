@@ -65,7 +65,7 @@ def test_pool_and_server_host_checks(nsg):
     assert nsg.nsg_pool_destroy(None) == _lib.ERR_ARG
     assert nsg.nsg_server_destroy(None) == _lib.ERR_ARG
     assert nsg.nsg_segment_nuclei_batch(None, None, 0, None, 0) == _lib.ERR_ARG
-    t = _lib.Tuning(0, 0)
+    t = _lib.Tuning(0, 0, -1)
     assert nsg.nsg_context_set_tuning(None, C.byref(t)) == _lib.ERR_ARG
     assert nsg.nsg_pool_set_tuning(None, C.byref(t)) == _lib.ERR_ARG
     assert nsg.nsg_pool_set_timing(None, 1) == _lib.ERR_ARG

@@ -75,13 +75,15 @@ def test_imreconstruct_u8(cuda, orc, shape, conn):
                                   orc.imreconstruct(marker, mask, conn))
 
 
+@pytest.mark.parametrize("wl", ["0", "1"])
 @pytest.mark.parametrize("shape", [(300, 517), (1024, 777)])
 @pytest.mark.parametrize("conn", [4, 8])
-def test_imreconstruct_u8_rough(cuda, orc, shape, conn):
+def test_imreconstruct_u8_rough(cuda, orc, shape, conn, wl, monkeypatch):
     """Per-pixel random mask and sparse seeds: propagation follows single-pixel
     (often diagonal) paths across many tiles, the case that exercises the
     dirty-line and neighbour-notification rules (smooth masks rarely do)."""
     from nscale_gb300 import morphologic_operations as MO
+    monkeypatch.setenv("NSG_RECON_WL", wl)
     g = np.random.default_rng(0x5EED0041 + shape[0] + conn)
     mask = g.integers(0, 256, size=shape).astype(np.uint8)
     marker = np.where(g.random(shape) < 0.01, mask, 0).astype(np.uint8)
@@ -96,6 +98,7 @@ def test_imreconstruct_u8_rough(cuda, orc, shape, conn):
     {"NSG_RECON_SEQMIN": "1"}, {"NSG_RECON_SEQMIN": "33"}, {"NSG_RECON_CTAS_PER_SM": "1"},
     {"NSG_RECON_HYB": "0"}, {"NSG_RECON_HYB": "0", "NSG_RECON_MINB": "2"}, {"NSG_RECON_WARPS": "16"},
     {"NSG_RECON_WARPS": "32"}, {"NSG_RECON_PACKED": "1", "NSG_RECON_HYB": "0"}, {"NSG_RECON_MAX_CTAS": "3"},
+    {"NSG_RECON_WL": "1"}, {"NSG_RECON_WL": "1", "NSG_RECON_WLPH": "3"}, {"NSG_RECON_WL": "1", "NSG_RECON_MAX_CTAS": "2"},
 ])
 @pytest.mark.parametrize("conn", [4, 8])
 def test_imreconstruct_u8_launch_forms(cuda, orc, conn, knobs, monkeypatch):
@@ -108,11 +111,13 @@ def test_imreconstruct_u8_launch_forms(cuda, orc, conn, knobs, monkeypatch):
                                   orc.imreconstruct(marker, mask, conn))
 
 
+@pytest.mark.parametrize("wl", ["0", "1"])
 @pytest.mark.parametrize("shape", [(1, 1), (37, 1), (64, 64), (97, 131), (600, 700)])
 @pytest.mark.parametrize("conn", [4, 8])
-def test_imreconstruct_f32(cuda, orc, shape, conn):
+def test_imreconstruct_f32(cuda, orc, shape, conn, wl, monkeypatch):
     from nscale_gb300 import morphologic_operations as MO
     from nscale_gb300 import synth
+    monkeypatch.setenv("NSG_RECON_WL", wl)
     marker, mask = synth.recon_inputs_f32(*shape, seed=0x5EED0011 + shape[0])
     # signed values exercise the zero ring
     marker = marker - np.float32(100.0)
@@ -390,7 +395,7 @@ def test_invert_all_types(cuda, n):
     around the 16-byte vector width and on views that start off a 16-byte
     boundary (element tail path)."""
     import torch
-    from nscale_gb300.histological_entities import HistologicalEntities as HE
+    from nscale_gb300.histological_entities import PixelOperations as PO
     g = np.random.default_rng(n)
     u8 = g.integers(0, 256, size=n + 3).astype(np.uint8)
     i32 = g.integers(-2 ** 31, 2 ** 31, size=n + 3, dtype=np.int64).astype(np.int32)
@@ -401,11 +406,11 @@ def test_invert_all_types(cuda, n):
                     (f32, (-f32 + np.float32(0)).astype(np.float32))):
         t = torch.from_numpy(a).cuda()
         for off in (0, 1):
-            got = N(HE.invert(t[off:off + n]))
+            got = N(PO.invert(t[off:off + n]))
             assert got.dtype == a.dtype
             np.testing.assert_array_equal(got, want[off:off + n])
     with pytest.raises(TypeError):
-        HE.invert(torch.zeros(4, dtype=torch.float64, device="cuda"))
+        PO.invert(torch.zeros(4, dtype=torch.float64, device="cuda"))
 
 
 def test_segment_nuclei_host_entry(cuda, orc):

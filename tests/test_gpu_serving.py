@@ -152,11 +152,73 @@ def test_tuning_changes_no_result(cuda):
         tuned = pool.segment(tiles)
         stages, timed = pool.stage_times()
         pool.set_timing(False)
+        # the reconstruction's scan-to-queue switchover, another tuning knob
+        pool.set_tuning(recon_max_ctas=5, bfs_max_cluster=16, recon_wl_phases=2)
+        queued = pool.segment(tiles)
     finally:
         pool.close()
-    for (s0, l0, n0, b0), (s1, l1, n1, b1) in zip(base, tuned):
-        assert s0 == s1 and n0 == n1
+    for (s0, l0, n0, b0), (s1, l1, n1, b1), (s2, l2, n2, b2) in zip(base, tuned, queued):
+        assert s0 == s1 == s2 and n0 == n1 == n2
         assert torch.equal(l0, l1) and np.array_equal(b0, b1)
+        assert torch.equal(l0, l2) and np.array_equal(b0, b2)
     # per-stage timing of the pool's workers: every tile timed, the heavy stages seen
     assert timed == len(tiles)
     assert stages["reconToNuclei"] > 0 and stages["watershed"] > 0
+
+
+def test_server_size_classes_route_and_match(cuda):
+    """A server with workers in size classes: every tile runs on a context
+    that holds it (small tiles do not need a large context), results equal
+    the per-tile call's, and a tile no class holds is refused up front."""
+    from nscale_gb300 import _lib
+    from nscale_gb300.serving import TileServer
+    tiles = _tiles()
+    want = [_single(t) for t in tiles]
+    L = _lib.load()
+    small, big = (640, 640), (1024, 1500)
+    budget = 2 * L.nsg_pool_context_bytes(*small) + 2 * L.nsg_pool_context_bytes(*big)
+    srv = TileServer(0, 0, budget, queue_cap=64, classes=[small, big], weights=[1.0, 1.0])
+    try:
+        cw = srv.class_workers()
+        assert cw[small] >= 1 and cw[big] >= 1, cw
+        with pytest.raises(_lib.NsgError) as e:
+            srv.submit(np.zeros((2000, 2000, 3), np.uint8))
+        assert e.value.code == _lib.ERR_OOM
+        tick = {}
+        for i, t in enumerate(tiles * 2):
+            lab = np.empty(t.shape[:2], np.int32)
+            tick[srv.submit(t, lab, want_bbox=True)] = (i % len(tiles), lab)
+        got = []
+        while len(got) < len(tick):
+            got += srv.poll(16, 60000)
+        for r in got:
+            i, lab = tick[r["ticket"]]
+            ws, wl, wn, wb = want[i]
+            assert r["status"] == ws and r["compcount"] == wn
+            assert np.array_equal(lab, wl) and np.array_equal(r["bbox"], wb)
+    finally:
+        srv.close()
+
+
+def test_server_budget_split_over_classes(cuda):
+    """The budget buys workers in proportion to weight x context bytes, and
+    the largest class always gets one."""
+    from nscale_gb300 import _lib
+    from nscale_gb300.serving import TileServer
+    L = _lib.load()
+    a, b = (512, 512), (1024, 1024)
+    pa, pb = L.nsg_pool_context_bytes(*a), L.nsg_pool_context_bytes(*b)
+    srv = TileServer(0, 0, 4 * pa + 2 * pb, queue_cap=8, classes=[a, b], weights=[1.0, 1.0])
+    try:
+        cw = srv.class_workers()
+        assert cw[b] >= 1 and cw[a] >= 1
+        assert cw[a] * pa + cw[b] * pb <= 4 * pa + 2 * pb
+    finally:
+        srv.close()
+    # a budget that holds only one large context: one large worker
+    srv = TileServer(0, 0, pb + pa // 2, queue_cap=8, classes=[a, b], weights=[10.0, 1.0])
+    try:
+        cw = srv.class_workers()
+        assert cw[b] == 1
+    finally:
+        srv.close()

@@ -11,6 +11,12 @@ point.  This model applies exactly those rules, one line at a time (the
 lane-per-line scan: raster then anti-raster step, neighbours read as they are)
 and tiles in a random order, with small tiles so that propagation crosses many
 of them, and compares with the oracle's reconstruction.
+
+The worklist form (the default) is modelled too: a whole-tile pass runs one
+row + column phase pair and then a pixel worklist seeded with the pixels the
+column phase changed; a pass for changed halo sides skips the phases and
+seeds the worklist from the edge pixels those sides can raise.  Pixels are
+popped in random order (the kernel's warps take them in any order).
 """
 import random
 
@@ -24,7 +30,32 @@ def clamp(x, lo, hi):
     return min(max(x, lo), hi)
 
 
-def tile_pass(out, mask, ty, tx, TH, TW, conn8, dirty_in, rng):
+def worklist(o, hm, seeds, TH, TW, conn8, rng):
+    """Pop pixels (tile coordinates + 1) in random order; raise in-tile
+    neighbours below min(popped value, their mask) and queue them."""
+    queued = set(seeds)
+    changed = False
+    while queued:
+        p = rng.choice(sorted(queued))
+        queued.discard(p)
+        y, x = p
+        v = o[y, x]
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                if (dy == 0 and dx == 0) or (not conn8 and dy and dx):
+                    continue
+                qy, qx = y + dy, x + dx
+                if not (1 <= qy <= TH and 1 <= qx <= TW):
+                    continue
+                cand = min(v, hm[qy, qx])
+                if o[qy, qx] < cand:
+                    o[qy, qx] = cand
+                    queued.add((qy, qx))
+                    changed = True
+    return changed
+
+
+def tile_pass(out, mask, ty, tx, TH, TW, conn8, dirty_in, rng, wl=False, wl_phases=1):
     """One pass over tile (ty, tx); returns the neighbours to queue as (dy, dx, edge line)."""
     H, W = out.shape
     y0, x0 = ty * TH, tx * TW
@@ -49,7 +80,12 @@ def tile_pass(out, mask, ty, tx, TH, TW, conn8, dirty_in, rng):
     if dirty_in & D_E:
         dcol.add(TW - 1)
     anych = False
-    while True:
+    phases = not wl or bool(dirty_in & D_ALL)
+    it = 0
+    need_wl = False
+    while phases:
+        it += 1
+        cbm = set()  # pixels the column phase changes
         rows, drow = sorted(drow), set()
         rng.shuffle(rows)
         for r in rows:
@@ -88,6 +124,7 @@ def tile_pass(out, mask, ty, tx, TH, TW, conn8, dirty_in, rng):
                     o[y, C] = v
                     drow |= {y - 2, y - 1, y} & set(range(TH))
                     chc = anych = True
+                    cbm.add((y, C))
                 prev = v
             nxt = o[TH + 1, C]
             for y in range(TH, 0, -1):
@@ -96,9 +133,36 @@ def tile_pass(out, mask, ty, tx, TH, TW, conn8, dirty_in, rng):
                     o[y, C] = v
                     drow |= {y - 2, y - 1, y} & set(range(TH))
                     chc = anych = True
+                    cbm.add((y, C))
                 nxt = v
         if not chc:
             break
+        if wl and it == wl_phases:
+            need_wl = True
+            break
+    if wl:
+        seeds = set()
+        if need_wl:
+            seeds = cbm
+        elif not phases:
+            c8 = 1 if conn8 else 0
+            sides = []
+            if dirty_in & D_N:
+                sides += [((1, x), [(0, x + d) for d in range(-c8, c8 + 1)]) for x in range(1, TW + 1)]
+            if dirty_in & D_S:
+                sides += [((TH, x), [(TH + 1, x + d) for d in range(-c8, c8 + 1)]) for x in range(1, TW + 1)]
+            if dirty_in & D_W:
+                sides += [((y, 1), [(y + d, 0) for d in range(-c8, c8 + 1)]) for y in range(1, TH + 1)]
+            if dirty_in & D_E:
+                sides += [((y, TW), [(y + d, TW + 1) for d in range(-c8, c8 + 1)]) for y in range(1, TH + 1)]
+            for (qy, qx), halo in sides:
+                best = max(min(o[h], hm[qy, qx]) for h in halo)
+                if o[qy, qx] < best:
+                    o[qy, qx] = best
+                    seeds.add((qy, qx))
+                    anych = True
+        if seeds and worklist(o, hm, seeds, TH, TW, conn8, rng):
+            anych = True
     # neighbours to queue: a changed edge pixel above a halo pixel that is below its mask
     notes = []
     if anych:
@@ -135,7 +199,7 @@ def tile_pass(out, mask, ty, tx, TH, TW, conn8, dirty_in, rng):
     return notes
 
 
-def reconstruct_model(marker, mask, conn, TH, TW, rng):
+def reconstruct_model(marker, mask, conn, TH, TW, rng, wl=False, wl_phases=1):
     H, W = mask.shape
     out = np.minimum(marker, mask).astype(np.int64)
     m = mask.astype(np.int64)
@@ -146,7 +210,7 @@ def reconstruct_model(marker, mask, conn, TH, TW, rng):
     while queue:
         t = queue.pop(rng.randrange(len(queue)))  # any tile that is queued, in any order
         bits = dirty.pop(t)
-        for dy, dx, edge in tile_pass(out, m, t[0], t[1], TH, TW, conn == 8, bits, rng):
+        for dy, dx, edge in tile_pass(out, m, t[0], t[1], TH, TW, conn == 8, bits, rng, wl, wl_phases):
             nt = (t[0] + dy, t[1] + dx)
             if 0 <= nt[0] < ty_n and 0 <= nt[1] < tx_n:
                 if nt not in dirty:
@@ -155,9 +219,10 @@ def reconstruct_model(marker, mask, conn, TH, TW, rng):
     return out.astype(np.uint8)
 
 
+@pytest.mark.parametrize("form", ["phases", "worklist", "worklist2"])
 @pytest.mark.parametrize("conn", [4, 8])
 @pytest.mark.parametrize("shape,tile", [((37, 53), (8, 8)), ((64, 40), (16, 8)), ((29, 61), (8, 16))])
-def test_tile_queue_reaches_the_fixed_point(orc, conn, shape, tile):
+def test_tile_queue_reaches_the_fixed_point(orc, form, conn, shape, tile):
     from nscale_gb300 import synth
     rng = random.Random(0x5EED00C0 + conn + shape[0])
     for seed in range(4):
@@ -169,5 +234,6 @@ def test_tile_queue_reaches_the_fixed_point(orc, conn, shape, tile):
             marker = mask.copy()
         # sparse seeds make long winding propagation across many tiles
         marker = np.where(g.random(shape) < 0.02, marker, 0).astype(np.uint8)
-        got = reconstruct_model(marker, mask, conn, tile[0], tile[1], rng)
+        got = reconstruct_model(marker, mask, conn, tile[0], tile[1], rng, wl=form != "phases",
+                                wl_phases=2 if form == "worklist2" else 1)
         np.testing.assert_array_equal(got, orc.imreconstruct(marker, mask, conn))
