@@ -225,6 +225,24 @@ int nsg_stain_matrix(const double *M9, const uint8_t *b3, float *Q6);
 int nsg_color_deconv(nsg_context *ctx, const uint8_t *bgr, int rows, int cols, size_t row_stride_bytes,
                      const float *Q6, uint8_t *H, uint8_t *E, nsg_stream_t stream);
 
+/* ---- colour normalisation (before segmentation) --------------------------- */
+/* nscale::Normalization::targetParameters (Normalization.cpp:520-577): the
+ * mean and std of the lab channels of the pixels its Fisher discriminant
+ * calls foreground (HOST float[3] outputs).  Synchronises the stream. */
+int nsg_color_target_parameters(nsg_context *ctx, const uint8_t *bgr, int rows, int cols, size_t row_stride_bytes,
+                                float *mean3, float *std3, nsg_stream_t stream);
+/* nscale::Normalization::normalization(originalI, targetMean, targetStd)
+ * (Normalization.cpp:487-517): foreground pixels moved in lab space from
+ * their own mean / std to the target's (HOST float[3] inputs, e.g. from
+ * nsg_color_target_parameters on a target tile), every pixel back to BGR;
+ * out_bgr is a DEVICE rows x cols x 3 uint8 buffer (dense).  FP32 as the
+ * reference; an output level may differ by one from a CPU evaluation where a
+ * value sits on a rounding boundary (log10f / powf last bits).  Synchronises
+ * the stream. */
+int nsg_color_normalization(nsg_context *ctx, const uint8_t *bgr, int rows, int cols, size_t row_stride_bytes,
+                            const float *target_mean3, const float *target_std3, uint8_t *out_bgr,
+                            nsg_stream_t stream);
+
 /* ---- per-nucleus features (the serving output) ---------------------------- */
 /* Operators::gradient (Operators.cpp:568-640): |grad| of a uint8 image,
  * central differences with one-sided ones at the edges, rounded to uint8. */

@@ -94,6 +94,10 @@ _SIGS = {
     "nsg_stain_matrix": (_I, [_P, _P, C.POINTER(C.c_float)]),
     "nsg_color_deconv": (_I, [_P, _P, _I, _I, C.c_size_t, C.POINTER(C.c_float), _P, _P, _P]),
     "nsg_gradient_u8": (_I, [_P, _P, _P, _I, _I, _P]),
+    "nsg_color_target_parameters": (_I, [_P, _P, _I, _I, C.c_size_t, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                         _P]),
+    "nsg_color_normalization": (_I, [_P, _P, _I, _I, C.c_size_t, C.POINTER(C.c_float), C.POINTER(C.c_float), _P,
+                                     _P]),
     "nsg_nucleus_features": (_I, [_P, _P, _P, _I, _I, _P, _I, C.POINTER(_I), _P]),
     "nsg_pool_create": (_I, [C.POINTER(_P), _I, _I, _I, _I]),
     "nsg_pool_destroy": (_I, [_P]),

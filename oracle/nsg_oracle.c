@@ -1165,6 +1165,140 @@ void orc_color_deconv_f64(const uint8_t *bgr, int rows, int cols, const double *
 }
 
 /* ------------------------------------------------------------------------- */
+/* Colour normalisation (src/normalization/Normalization.cpp): Reinhard     */
+/* colour transfer in lab space of the foreground found by a Fisher          */
+/* discriminant.  The arithmetic follows the reference's order and widths:   */
+/* float where it computes on float Mats, double where it uses double        */
+/* literals or accumulators.  Restated, unpinned (OpenCV's MatExpr            */
+/* evaluation is part of it).                                                 */
+/* ------------------------------------------------------------------------- */
+
+/* discriminant coefficients M (Normalization.cpp:504-505, 555-556) */
+static const float kNormM[8] = {-0.154f, 0.035f, 0.549f, -45.718f, -0.057f, -0.817f, 1.170f, -49.887f};
+
+/* segFG (Normalization.cpp:19-55): d_k = M(k,0) R + M(k,1) G + M(k,2) B +
+ * M(k,3) evaluated as OpenCV 2.4 evaluates the MatExpr: addWeighted of the
+ * first two products, then addWeighted of that and the third with the
+ * constant as gamma, each computed in double and stored as float;
+ * foreground = d1 < d2. */
+static int norm_fg(const uint8_t *px) {
+    const float bd = (float)px[0], gd = (float)px[1], rd = (float)px[2];
+    float d[2];
+    for (int k = 0; k < 2; ++k) {
+        const float *m = kNormM + 4 * k;
+        const float t = (float)((double)rd * (double)m[0] + (double)gd * (double)m[1] + 0.0);
+        d[k] = (float)((double)t * 1.0 + (double)bd * (double)m[2] + (double)m[3]);
+    }
+    return d[0] < d[1];
+}
+
+/* bgr2Lab (Normalization.cpp:64-149) of one pixel of I / 255 (convertTo,
+ * then the Mat divided by 255: a float scale by (float)(1 / 255.0)) */
+static void norm_lab(const uint8_t *px, float lab[3]) {
+    const float s = (float)(1.0 / 255.0);
+    const float b = (float)px[0] * s, g = (float)px[1] * s, r = (float)px[2] * s;
+    const float L = (float)(0.3811 * r + 0.5783 * g + 0.0402 * b);
+    const float M = (float)(0.1967 * r + 0.7244 * g + 0.0782 * b);
+    const float S = (float)(0.0241 * r + 0.1288 * g + 0.8444 * b);
+    const float l = log10f(L), m = log10f(M), sl = log10f(S);
+    const float i3 = 1 / sqrtf(3.0f), i6 = 1 / sqrtf(6.0f), i2 = 1 / sqrtf(2.0f);
+    /* Matrix2 = diag(1/sqrt3, 1/sqrt6, 1/sqrt2) * [1 1 1; 1 1 -2; 1 -1 0] */
+    lab[0] = l * i3 + m * i3 + sl * i3;
+    lab[1] = l * i6 + m * i6 + sl * (-2.0f * i6);
+    lab[2] = l * i2 + m * (-i2) + sl * 0.0f;
+}
+
+static int norm_rndint(float n) { /* Normalization.cpp:153-162 */
+    int ret = (int)floor(n);
+    float t = n - (float)floor(n);
+    if (t >= 0.5) ret = (int)floor(n) + 1;
+    return ret;
+}
+
+/* lab2BGR (Normalization.cpp:166-292) of one pixel */
+static void norm_bgr(const float lab[3], uint8_t *out) {
+    const float i3 = 1 / sqrtf(3.0f), i6 = 1 / sqrtf(6.0f), i2 = 1 / sqrtf(2.0f);
+    /* Matrix1 = [1 1 1; 1 1 -1; 1 -2 0] * diag(1/sqrt3, 1/sqrt6, 1/sqrt2) */
+    const float l = lab[0], a = lab[1], b = lab[2];
+    float lms[3];
+    lms[0] = l * i3 + a * i6 + b * i2;
+    lms[1] = l * i3 + a * i6 + b * (-i2);
+    lms[2] = l * i3 + a * (-2.0f * i6) + b * 0.0f;
+    for (int c = 0; c < 3; ++c) {
+        float x = powf(10.0f, lms[c]);
+        if (!(x <= DBL_MAX && x >= -DBL_MAX)) x = 0.0f; /* -Inf / NaN -> 0 */
+        lms[c] = x;
+    }
+    static const float M2[9] = {4.4687f, -3.5887f, 0.1196f, -1.2197f, 2.3831f, -0.1626f, 0.0585f, -0.2611f, 1.2057f};
+    const float L = lms[0], M = lms[1], S = lms[2];
+    const float bf = L * M2[6] + M * M2[7] + S * M2[8];
+    const float gf = L * M2[3] + M * M2[4] + S * M2[5];
+    const float rf = L * M2[0] + M * M2[1] + S * M2[2];
+    const float v[3] = {bf, gf, rf};
+    for (int c = 0; c < 3; ++c) {
+        float sc = (float)(v[c] * 255.0);
+        if (sc < 0.0) sc = 0.0f;
+        if (sc > 255.0) sc = 255.0f;
+        out[c] = (uint8_t)norm_rndint(sc);
+    }
+}
+
+/* the foreground's lab statistics (TransferI / targetParameters,
+ * Normalization.cpp:296-350, 520-577): over foreground pixels whose
+ * L * a * b product (float) is positive, sum and sum of squares (the square
+ * in float, the sums in double), mean = sum / n, std = sqrt(sq / n - mean^2) */
+void orc_norm_stats(const uint8_t *bgr, int rows, int cols, double *count, double *sum3, double *sq3) {
+    const int64_t n = (int64_t)rows * cols;
+    double c = 0.0, s[3] = {0, 0, 0}, q[3] = {0, 0, 0};
+    for (int ch = 0; ch < 3; ++ch) { /* the reference sums channel by channel */
+        for (int64_t i = 0; i < n; ++i) {
+            const uint8_t *px = bgr + 3 * i;
+            if (!norm_fg(px)) continue;
+            float lab[3];
+            norm_lab(px, lab);
+            if (!((lab[0] * lab[1]) * lab[2] > 0)) continue;
+            s[ch] += lab[ch];
+            q[ch] += lab[ch] * lab[ch];
+            if (ch == 0) c += 1.0;
+        }
+    }
+    *count = c;
+    for (int k = 0; k < 3; ++k) sum3[k] = s[k], sq3[k] = q[k];
+}
+
+/* Normalization::targetParameters (Normalization.cpp:520-577) */
+void orc_target_parameters(const uint8_t *bgr, int rows, int cols, float *mean3, float *std3) {
+    double c, s[3], q[3];
+    orc_norm_stats(bgr, rows, cols, &c, s, q);
+    for (int k = 0; k < 3; ++k) {
+        const double mean = s[k] / c;
+        const double var = q[k] / c - mean * mean;
+        mean3[k] = (float)mean;
+        std3[k] = (float)sqrt(var);
+    }
+}
+
+/* Normalization::normalization (Normalization.cpp:487-517): foreground lab
+ * values mapped by (v - mean) * (stdT / std) + meanT (float), background lab
+ * kept, every pixel back through lab2BGR. */
+void orc_normalization(const uint8_t *bgr, int rows, int cols, const float *meanT, const float *stdT,
+                       uint8_t *out) {
+    float meanL[3], stdL[3];
+    orc_target_parameters(bgr, rows, cols, meanL, stdL);
+    float ratio[3];
+    for (int k = 0; k < 3; ++k) ratio[k] = stdT[k] / stdL[k];
+    const int64_t n = (int64_t)rows * cols;
+    for (int64_t i = 0; i < n; ++i) {
+        const uint8_t *px = bgr + 3 * i;
+        float lab[3];
+        norm_lab(px, lab);
+        if (norm_fg(px))
+            for (int k = 0; k < 3; ++k) lab[k] = (lab[k] - meanL[k]) * ratio[k] + meanT[k];
+        norm_bgr(lab, out + 3 * i);
+    }
+}
+
+/* ------------------------------------------------------------------------- */
 /* Per-nucleus features (src/features/ObjFeatures.cpp, Operators.cpp).       */
 /* ------------------------------------------------------------------------- */
 

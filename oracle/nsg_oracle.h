@@ -123,6 +123,14 @@ void orc_color_deconv(const uint8_t *bgr, int rows, int cols, const float *Q6, c
                       uint8_t *E);
 void orc_color_deconv_f64(const uint8_t *bgr, int rows, int cols, const double *Q6, uint8_t *H, uint8_t *E);
 
+/* Colour normalisation (src/normalization/Normalization.cpp): foreground
+ * lab statistics, targetParameters (mean, std of the foreground's lab
+ * channels) and normalization (Reinhard transfer to meanT / stdT). */
+void orc_norm_stats(const uint8_t *bgr, int rows, int cols, double *count, double *sum3, double *sq3);
+void orc_target_parameters(const uint8_t *bgr, int rows, int cols, float *mean3, float *std3);
+void orc_normalization(const uint8_t *bgr, int rows, int cols, const float *meanT, const float *stdT,
+                       uint8_t *out);
+
 /* Per-nucleus features of the serving output (src/features): gradient
  * magnitude image (Operators.cpp:568-640) and, per label in bounding-box
  * order, {area, perimeter, mean H, std H, mean gradient of H} as float. */

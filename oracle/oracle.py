@@ -97,6 +97,8 @@ def lib():
         L.orc_color_deconv.argtypes = [_u8p, C.c_int, C.c_int, _f32p, _f32p, _u8p, _u8p]
         L.orc_color_deconv_f64.argtypes = [_u8p, C.c_int, C.c_int, _f64p, _u8p, _u8p]
         L.orc_gradient_u8.argtypes = [_u8p, C.c_int, C.c_int, _u8p]
+        L.orc_target_parameters.argtypes = [_u8p, C.c_int, C.c_int, _f32p, _f32p]
+        L.orc_normalization.argtypes = [_u8p, C.c_int, C.c_int, _f32p, _f32p, _u8p]
         L.orc_nucleus_features.argtypes = [_i32p, _u8p, C.c_int, C.c_int, _f32p]
         L.orc_nucleus_features.restype = C.c_int
         L.orc_erode_u8.argtypes = [_u8p, C.c_int, C.c_int, _u8p, C.c_int, _u8p]
@@ -264,6 +266,23 @@ def color_deconv(bgr, Q=None, f64=False):
         lib().orc_color_deconv(bgr, bgr.shape[0], bgr.shape[1], _c(Qd.astype(np.float32), np.float32).ravel(),
                                color_lut(), H, E)
     return H, E
+
+
+def target_parameters(bgr):
+    """Normalization::targetParameters: (mean[3], std[3]) float32."""
+    bgr = _c(bgr, np.uint8)
+    m, sd = np.empty(3, np.float32), np.empty(3, np.float32)
+    lib().orc_target_parameters(bgr, bgr.shape[0], bgr.shape[1], m, sd)
+    return m, sd
+
+
+def normalization(bgr, mean_t, std_t):
+    """Normalization::normalization: the BGR tile moved to the target's lab
+    statistics."""
+    bgr = _c(bgr, np.uint8)
+    out = np.empty_like(bgr)
+    lib().orc_normalization(bgr, bgr.shape[0], bgr.shape[1], _c(mean_t, np.float32), _c(std_t, np.float32), out)
+    return out
 
 
 def gradient(img):

@@ -440,3 +440,33 @@ def test_segment_nuclei_host_entry(cuda, orc):
     st = big.L.nsg_segment_nuclei_host(big.h, img.ctypes.data, big.max_rows + 1, big.max_cols + 1, None, None,
                                        None, None, None, stream_handle())
     assert st == _lib.ERR_OOM
+
+
+@pytest.mark.parametrize("shape", [(1, 7), (97, 131), (512, 700), (4096, 4096)])
+def test_color_normalization(cuda, orc, shape):
+    """Normalization::targetParameters / normalization on the GPU against the
+    oracle: statistics within 1e-5 relative; output levels within one, on at
+    most 0.1 % of the values (log10f / powf last bits on a rounding boundary),
+    and a tile normalised to its own statistics comes back unchanged."""
+    import torch
+    from nscale_gb300 import synth_torch
+    from nscale_gb300.normalization import Normalization
+    img_t = synth_torch.he_tile(*shape, 0x5EED0500 + shape[0], device="cuda")
+    tgt_t = synth_torch.he_tile(256, 256, 0x5EED0501, device="cuda")
+    img, tgt = img_t.cpu().numpy(), tgt_t.cpu().numpy()
+    m, s = Normalization.targetParameters(img_t)
+    om, os_ = orc.target_parameters(img)
+    if np.isfinite(om).all():
+        np.testing.assert_allclose(m, om, rtol=1e-5, atol=1e-7)
+        np.testing.assert_allclose(s, os_, rtol=1e-5, atol=1e-7)
+    mt, st = orc.target_parameters(tgt)
+    got = N(Normalization.normalization(img_t, mt, st))
+    want = orc.normalization(img, mt, st)
+    d = np.abs(got.astype(np.int16) - want.astype(np.int16))
+    assert d.max() <= 1, d.max()
+    assert (d > 0).mean() <= 1e-3, (d > 0).mean()
+    if shape[0] > 1:
+        same = N(Normalization.normalization(img_t, m, s))
+        dd = np.abs(same.astype(np.int16) - img.astype(np.int16))
+        assert dd.max() <= 1 and (dd > 0).mean() <= 1e-3
+    torch.cuda.synchronize()

@@ -262,3 +262,18 @@ def test_features_count_form_matches_reference_order(orc):
         per = (c == 1).sum() * 0.70710678118 + (c == 2).sum() * 1.0 + (c == 3).sum() * 1.41421356237
         assert abs(per - f[k, 1]) <= 1e-5 * max(1.0, per)
         assert f[k, 0] == (lab == L).sum()
+
+
+def test_normalization_to_own_statistics_is_identity(orc):
+    """Colour normalisation towards a tile's own foreground statistics maps the
+    tile onto itself (the lab round trip and rndint give back every level),
+    and towards another tile's statistics moves the foreground only."""
+    from nscale_gb300 import synth
+    img = synth.he_tile(300, 400, seed=5)
+    m, s = orc.target_parameters(img)
+    assert np.all(np.isfinite(m)) and np.all(s > 0)
+    np.testing.assert_array_equal(orc.normalization(img, m, s), img)
+    mt, st = orc.target_parameters(synth.he_tile(200, 200, seed=77))
+    out = orc.normalization(img, mt, st)
+    assert out.shape == img.shape and out.dtype == np.uint8
+    assert (out != img).any()
