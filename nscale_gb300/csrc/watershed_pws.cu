@@ -80,6 +80,7 @@ enum {
     W_LAYERS,
     W_BFSCTAS,
     W_DTOT,  // dummy slots reserved over all domains
+    W_NORD,  // entries of the size-ordered dispatch list (PW::ord)
 };
 
 struct PW {
@@ -104,6 +105,9 @@ struct PW {
     // per domain: dummy slots reserved (distinct U pixels beside it) and where they start;
     // alias the root flags / root ranks, which are free once the domains are numbered
     int *ducnt, *duoff;
+    // size-ordered dispatch of the per-domain (P1) and per-group (P3) floods:
+    // the ids by decreasing work class, each id's class, 32 class counts + 32 offsets
+    int *ord, *okey, *obucket;
 };
 
 // A pop's reads, issued together: the four neighbours' flags, markers,
@@ -279,13 +283,61 @@ __device__ __forceinline__ void q_push(Q &q, int *next, int lvl, int e) {
 constexpr int kP1Threads = 32, kQPitch = 513;
 constexpr size_t kP1Smem = sizeof(int) * kP1Threads * kQPitch;
 __device__ void phase1_domain(const PW &a, int d, Q &q);
+// Size-ordered dispatch.  A flood block holds its shared memory (32 queue
+// tables) until its longest flood ends, so blocks are filled with floods of
+// about the same length, longest first: the ids are bucketed by work class
+// (the leading-zero count of the work: a factor of two per class) and thread
+// t of the launch takes the t-th id.  Which thread floods which domain does
+// not change any result (every flood writes only its own domain's records).
+// mode 0: domains, work = pixels + reserved dummy slots (P1);
+// mode 1: P3 groups (mcount > 0), work = their members' pixels.
+__device__ __forceinline__ int flood_work(const PW &a, int d, int mode) {
+    if (mode == 0) return a.dsize[d] + a.ducnt[d];
+    const int nm = a.mcount[d];
+    if (nm <= 0) return -1;
+    const int *mem = a.mlist + a.moff[d];
+    int w = 0;
+    for (int m = 0; m < nm; ++m) w += a.dsize[mem[m]];
+    return w;
+}
+__global__ void k_order_count(PW a, int mode) {
+    const int nd = a.ctl[W_ND];
+    for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < nd; d += gridDim.x * blockDim.x) {
+        const int w = flood_work(a, d, mode);
+        const int k = w < 0 ? -1 : __clz(w > 1 ? w : 1);
+        a.okey[d] = k;
+        if (k >= 0) atomicAdd(a.obucket + k, 1);
+    }
+}
+__global__ void k_order_scan(PW a) {  // one warp
+    const int lane = threadIdx.x;
+    const int v = a.obucket[lane];
+    int x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+    }
+    a.obucket[32 + lane] = x - v;  // exclusive offset of class `lane`
+    a.obucket[lane] = 0;           // reused as the fill counter
+    if (lane == 31) a.ctl[W_NORD] = x;
+}
+__global__ void k_order_scatter(PW a) {
+    const int nd = a.ctl[W_ND];
+    for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < nd; d += gridDim.x * blockDim.x) {
+        const int k = a.okey[d];
+        if (k >= 0) a.ord[a.obucket[32 + k] + atomicAdd(a.obucket + k, 1)] = d;
+    }
+}
+
 __global__ void __launch_bounds__(kP1Threads) k_phase1(PW a) {
     extern __shared__ int qsm[];
-    const int nd = a.ctl[W_ND];
+    const int nd = a.ctl[W_NORD];
     Q q;
     q.h = qsm + threadIdx.x * kQPitch;
     q.t = q.h + 256;
-    for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < nd; d += gridDim.x * blockDim.x) phase1_domain(a, d, q);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nd; t += gridDim.x * blockDim.x)
+        phase1_domain(a, a.ord[t], q);
 }
 
 __device__ void phase1_domain(const PW &a, int d, Q &q) {
@@ -1150,13 +1202,13 @@ __device__ void queue_at_te(const PW &a, int d, Q &q) {
 __device__ void phase3_group(const PW &a, int S, Q &q);
 __global__ void __launch_bounds__(kP1Threads) k_phase3(PW a) {
     extern __shared__ int qsm[];
-    const int nd = a.ctl[W_ND];
+    const int ng = a.ctl[W_NORD];  // the groups, longest first (k_order_*, mode 1)
     if (a.ctl[W_FALLBACK] || !a.ctl[W_EVENT]) return;
     Q q;
     q.h = qsm + threadIdx.x * kQPitch;
     q.t = q.h + 256;
-    for (int S = blockIdx.x * blockDim.x + threadIdx.x; S < nd; S += gridDim.x * blockDim.x)
-        if (a.mcount[S] > 0) phase3_group(a, S, q);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ng; t += gridDim.x * blockDim.x)
+        phase3_group(a, a.ord[t], q);
 }
 __device__ void phase3_group(const PW &a, int S, Q &q) {
     const int nm = a.mcount[S];
@@ -1506,6 +1558,9 @@ void carve(PW &a, char *base, size_t *used_out) {
     a.pend = cv.take<int>(n);
     a.pend2 = cv.take<int>(n);
     a.dfirst = cv.take<unsigned long long>(n);
+    a.ord = cv.take<int>(n);
+    a.okey = cv.take<int>(n);
+    a.obucket = cv.take<int>(64);
     *used_out = cv.used;
 }
 
@@ -1575,6 +1630,33 @@ static int launch_bfs(Ctx &c, const PW &a, const uint8_t *nbm, cudaStream_t s) {
     return NSG_SUCCESS;
 }
 
+// The dispatch list of the P1 (mode 0) or P3 (mode 1) floods, longest
+// first, and its length on the host (*count; a readback, so this waits for
+// the stream).  The flood kernels are launched with exactly the blocks that
+// have floods: each block holds 32 queue tables of shared memory, and a
+// launch padded with empty blocks would wait, under load from the other
+// tiles in flight, until every empty block found that much free shared
+// memory on some SM.
+static int order_floods(Ctx &c, PW &a, int mode, int *count, cudaStream_t s) {
+    const int g = blocks(c, a.n);
+    NSG_CUDA_TRY(c, cudaMemsetAsync(a.obucket, 0, 64 * sizeof(int), s));
+    k_order_count<<<g, kB, 0, s>>>(a, mode);
+    NSG_COUNT_LAUNCH();
+    k_order_scan<<<1, 32, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
+    k_order_scatter<<<g, kB, 0, s>>>(a);
+    NSG_COUNT_LAUNCH();
+    NSG_LAUNCH_CHECK(c);
+    NSG_CUDA_TRY(c, cudaMemcpyAsync(c.ws.h_ctrl + C_WS + W_NORD, a.ctl + W_NORD, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NSG_CUDA_TRY(c, cudaStreamSynchronize(s));
+    *count = c.ws.h_ctrl[C_WS + W_NORD];
+    return NSG_SUCCESS;
+}
+static int flood_blocks(int count) {
+    const int b = (count + kP1Threads - 1) / kP1Threads;
+    return b < 1 ? 1 : b;
+}
+
 int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int W, cudaStream_t s) {
     PW a;
     a.H = H;
@@ -1616,8 +1698,10 @@ int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int 
     // per-domain kernels: grid-stride over the domain count (on the device); 64-thread
     // blocks, 4 per SM cover 38,912 domains at once (a 4096^2 tile has a few thousand)
     const int gd = c.sm_count * 4;
+    int nflood = 0;
+    NSG_TRY(order_floods(c, a, 0, &nflood, s));
     NSG_CUDA_TRY(c, cudaFuncSetAttribute(k_phase1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kP1Smem));
-    k_phase1<<<gd * 64 / kP1Threads, kP1Threads, kP1Smem, s>>>(a);
+    k_phase1<<<flood_blocks(nflood), kP1Threads, kP1Smem, s>>>(a);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     stage_mark(c, kStageWsP1, s);
@@ -1675,8 +1759,9 @@ int pws_flood(Ctx &c, const int *mk, const uint32_t *col, int *outp, int H, int 
     k_p3_state<<<g, kB, 0, s>>>(a);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
+    NSG_TRY(order_floods(c, a, 1, &nflood, s));
     NSG_CUDA_TRY(c, cudaFuncSetAttribute(k_phase3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kP1Smem));
-    k_phase3<<<gd * 64 / kP1Threads, kP1Threads, kP1Smem, s>>>(a);
+    k_phase3<<<flood_blocks(nflood), kP1Threads, kP1Smem, s>>>(a);
     NSG_COUNT_LAUNCH();
     stage_mark(c, kStageWsP3, s);
     k_assemble<<<g, kB, 0, s>>>(a);
