@@ -188,6 +188,9 @@ int front_rbc(Ctx &c, const uint8_t *bgr, int64_t row_stride, int rows, int cols
               uint8_t *rc, uint8_t *bw1, uint8_t *bw2, uint8_t *r2b, int *d_bw1_count, cudaStream_t s);
 int background_count(Ctx &c, const uint8_t *bgr, int64_t row_stride, int rows, int cols, int blue, int green,
                      int red, uint8_t *mask, int64_t *d_count, cudaStream_t s);
+int front_fused(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int cols, int blue, int green, int red,
+                double T1, double T2, int64_t *d_bg_count, uint8_t *rc, uint8_t *bw1, uint8_t *bw2, uint8_t *r2b,
+                int *d_bw1_count, cudaStream_t s);
 int diff_threshold(Ctx &c, const uint8_t *rc, const uint8_t *rc_recon, int rows, int cols, int G1, int G2,
                    uint8_t *bw_g1, uint8_t *bw_g2, cudaStream_t s);
 int and_not(Ctx &c, uint8_t *inout, const uint8_t *notmask, int64_t n, cudaStream_t s);

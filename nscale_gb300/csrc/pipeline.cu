@@ -158,8 +158,8 @@ int segment_nuclei_dev(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int
     } fin_timer{c, s};
 
     // ---- plFindNucleusCandidates --------------------------------------------
-    NSG_TRY(background_count(c, bgr, stride, rows, cols, p.blue, p.green, p.red, nullptr, c.ws.ctr64, s));
-    NSG_TRY(front_rbc(c, bgr, stride, rows, cols, p.T1, p.T2, P[0], P[1], P[2], P[3], ctrl + C_COUNT0, s));
+    NSG_TRY(front_fused(c, bgr, stride, rows, cols, p.blue, p.green, p.red, p.T1, p.T2, c.ws.ctr64, P[0], P[1], P[2],
+                        P[3], ctrl + C_COUNT0, s));
     t_mark(c, 0, s);
     // the background ratio decides before anything expensive runs (HE:123-137):
     // the readback waits only for the two front passes, and a tissue-free tile

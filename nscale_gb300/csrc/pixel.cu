@@ -78,6 +78,68 @@ __global__ void front_rbc_kernel(const uint8_t *__restrict__ bgr, int64_t stride
     }
 }
 
+// The front of segmentNuclei in one pass over the tile, 16 pixels per thread
+// with 128-bit accesses: three 16-byte loads of BGR, the background test
+// (HE:93-109, counted), getRBC's float32 ratios (HE:54-71) and the red
+// complement (HE:158) for the 16 pixels, four 16-byte stores.  Consecutive
+// threads take consecutive 16-pixel chunks of a row.  Needs cols % 16 == 0 and
+// a 16-byte aligned tile, row stride and outputs (front_fused checks).
+union V16 {
+    uint4 u;
+    uint8_t b[16];
+};
+__device__ __forceinline__ void front_px(uint8_t B, uint8_t G, uint8_t R, int blue, int green, int red, float t1,
+                                         float t2, unsigned &bg, uint8_t &rc, uint8_t &b1, uint8_t &b2,
+                                         uint8_t &r2b) {
+    bg += (B > blue && G > green && R > red) ? 1u : 0u;
+    const float bd = __fadd_rn((float)B, FLT_EPSILON);
+    const float gd = __fadd_rn((float)G, FLT_EPSILON);
+    const float rd = (float)R;
+    const float r2g = __fdiv_rn(rd, gd), rb = __fdiv_rn(rd, bd);
+    b1 = r2g > t1 ? 255 : 0;
+    b2 = r2g > t2 ? 255 : 0;
+    r2b = rb > 1.0f ? 255 : 0;
+    rc = (uint8_t)(255 - R);
+}
+__global__ void __launch_bounds__(256) front16_kernel(const uint8_t *__restrict__ bgr, int64_t stride, int rows,
+                                                      int cols, int blue, int green, int red, float t1, float t2,
+                                                      uint8_t *__restrict__ rc, uint8_t *__restrict__ bw1,
+                                                      uint8_t *__restrict__ bw2, uint8_t *__restrict__ r2b,
+                                                      unsigned long long *__restrict__ bg_count,
+                                                      int *__restrict__ bw1_count) {
+    const int64_t cpr = cols / 16, total = cpr * rows;
+    for (int64_t t0 = (int64_t)blockIdx.x * blockDim.x; t0 < total; t0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t t = t0 + threadIdx.x;
+        unsigned bg = 0, n1 = 0;
+        if (t < total) {
+            const int y = (int)(t / cpr);
+            const int x0 = (int)(t - (int64_t)y * cpr) * 16;
+            const uint4 *src = reinterpret_cast<const uint4 *>(bgr + (int64_t)y * stride + 3 * x0);
+            V16 in[3];
+            in[0].u = __ldg(src);
+            in[1].u = __ldg(src + 1);
+            in[2].u = __ldg(src + 2);
+            V16 o_rc, o_b1, o_b2, o_rb;
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
+                const int j = 3 * k;
+                const uint8_t B = in[j >> 4].b[j & 15], G = in[(j + 1) >> 4].b[(j + 1) & 15],
+                              R = in[(j + 2) >> 4].b[(j + 2) & 15];
+                front_px(B, G, R, blue, green, red, t1, t2, bg, o_rc.b[k], o_b1.b[k], o_b2.b[k], o_rb.b[k]);
+                n1 += o_b1.b[k] ? 1u : 0u;
+            }
+            const int64_t o = (int64_t)y * cols + x0;
+            *reinterpret_cast<uint4 *>(rc + o) = o_rc.u;
+            *reinterpret_cast<uint4 *>(bw1 + o) = o_b1.u;
+            *reinterpret_cast<uint4 *>(bw2 + o) = o_b2.u;
+            *reinterpret_cast<uint4 *>(r2b + o) = o_rb.u;
+        }
+        warp_add_u64(bg_count, bg);
+        for (int off = 16; off > 0; off >>= 1) n1 += __shfl_down_sync(0xffffffffu, n1, off);
+        if ((threadIdx.x & 31) == 0 && n1) atomicAdd(bw1_count, (int)n1);
+    }
+}
+
 __global__ void diff_threshold_kernel(const uint8_t *__restrict__ rc, const uint8_t *__restrict__ rec, int64_t n,
                                       int g1, int g2, uint8_t *__restrict__ o1, uint8_t *__restrict__ o2) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -174,6 +236,27 @@ int front_rbc(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int cols, do
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
+}
+
+// background count and the RBC front in one 128-bit pass where the layout
+// allows it, else the two scalar passes
+int front_fused(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int cols, int blue, int green, int red,
+                double T1, double T2, int64_t *d_bg_count, uint8_t *rc, uint8_t *bw1, uint8_t *bw2, uint8_t *r2b,
+                int *d_bw1_count, cudaStream_t s) {
+    const auto a16 = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+    if (cols % 16 == 0 && stride % 16 == 0 && a16(bgr) && a16(rc) && a16(bw1) && a16(bw2) && a16(r2b)) {
+        NSG_CUDA_TRY(c, cudaMemsetAsync(d_bg_count, 0, sizeof(int64_t), s));
+        NSG_CUDA_TRY(c, cudaMemsetAsync(d_bw1_count, 0, sizeof(int), s));
+        const int64_t chunks = (int64_t)(cols / 16) * rows;
+        front16_kernel<<<blocks_for(c, chunks), kBlock, 0, s>>>(bgr, stride, rows, cols, blue, green, red, (float)T1,
+                                                                (float)T2, rc, bw1, bw2, r2b,
+                                                                (unsigned long long *)d_bg_count, d_bw1_count);
+        NSG_COUNT_LAUNCH();
+        NSG_LAUNCH_CHECK(c);
+        return NSG_SUCCESS;
+    }
+    NSG_TRY(background_count(c, bgr, stride, rows, cols, blue, green, red, nullptr, d_bg_count, s));
+    return front_rbc(c, bgr, stride, rows, cols, T1, T2, rc, bw1, bw2, r2b, d_bw1_count, s);
 }
 
 int diff_threshold(Ctx &c, const uint8_t *rc, const uint8_t *rec, int rows, int cols, int G1, int G2, uint8_t *o1,

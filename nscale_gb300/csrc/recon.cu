@@ -31,6 +31,9 @@
 #include <float.h>
 #include <math.h>
 #include <stdlib.h>
+#include <string.h>
+
+#include <cuda.h>  // CUtensorMap (the encoder comes from the runtime's driver entry point)
 
 #include <type_traits>
 
@@ -790,6 +793,108 @@ __device__ void wl_seed_halo(TileWL<T, TW, TH, P> &sm, int dirty_in, bool conn8,
     __syncthreads();
 }
 
+
+// ---- TMA-fed tile load (uint8, 128 x 128 tiles) -----------------------------
+// One elected thread stages the tile's out plane and mask, each with a
+// one-pixel ring, into shared memory with two 2-D tensor copies
+// (cp.async.bulk.tensor) that complete on one mbarrier; the CTA waits on the
+// barrier (bounded) and unpacks the staging boxes into the padded tile
+// layout.  The boxes are 160 x 130 bytes starting at (x0 - 16, y0 - 1): the
+// innermost start coordinate stays a multiple of 16 bytes (x0 is a multiple
+// of 128), and samples outside the image read as 0, which is the
+// reconstruction's padding ring and the mask outside the image.  The host
+// only enables this when the row pitch and both base addresses are
+// multiples of 16 bytes (the tensor-map rules); otherwise the plain loads run.
+constexpr int kStW = 160, kStH = 130, kStageBytes = kStW * kStH;
+// a tensor copy's shared-memory destination must sit on a 128-byte boundary:
+// each staging box starts at one (20800 bytes rounded up to 20864)
+constexpr int kStagePitch = (kStageBytes + 127) & ~127;
+
+struct TmaArgs {
+    const CUtensorMap *out_map, *mask_map;  // the kernel's __grid_constant__ parameters
+    uint8_t *stage;                         // 2 boxes kStagePitch apart, 128-byte aligned
+    uint64_t *bar;                          // the copies' mbarrier
+    unsigned *phase;                        // its current phase parity
+    int on;
+};
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(a) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+// true when the phase with parity `parity` has completed within `budget` polls
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, long long budget) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+    for (long long k = 0; k <= budget; ++k) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void tma_load_2d(uint8_t *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst), b = (unsigned)__cvta_generic_to_shared(bar);
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(d), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(b)
+        : "memory");
+}
+
+// the tile (ty, tx) and its ring into `o` (pitch P), the mask into `m`, and
+// the mask just outside the tile into mN / mS / mW / mE; returns false when
+// the copies did not arrive within the budget (DEV_TIMEOUT is then set)
+template <int P>
+__device__ bool tma_tile_u8(const TmaArgs &ta, int tx, int ty, uint8_t *o, uint8_t *m, uint8_t *mN, uint8_t *mS,
+                            uint8_t *mW, uint8_t *mE, long long budget, int *status) {
+    constexpr int TW = 128, TH = 128;
+    const int x0 = tx * TW, y0 = ty * TH;
+    const unsigned parity = *ta.phase;
+    if (threadIdx.x == 0) {
+        // `out` was last written by generic stores (this CTA's or, before the
+        // queue handed the tile over, other CTAs'); the staging area was last
+        // read by generic loads: order both before the async-proxy copies
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(ta.bar, 2 * kStageBytes);
+        tma_load_2d(ta.stage, ta.out_map, x0 - 16, y0 - 1, ta.bar);
+        tma_load_2d(ta.stage + kStagePitch, ta.mask_map, x0 - 16, y0 - 1, ta.bar);
+    }
+    bool ok = mbar_wait(ta.bar, parity, budget);
+    if (!ok) {
+        atomicOr(status, DEV_TIMEOUT);
+        ok = mbar_wait(ta.bar, parity, budget);  // do not leave copies in flight into this CTA's memory
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *ta.phase = parity ^ 1u;
+    const uint8_t *so = ta.stage, *sk = ta.stage + kStagePitch;
+    for (int i = threadIdx.x; i < (TH + 2) * (TW + 2); i += blockDim.x) {
+        const int r = i / (TW + 2), c = i - r * (TW + 2);
+        o[r * P + c] = so[r * kStW + 15 + c];
+    }
+    for (int i = threadIdx.x; i < TH * TW; i += blockDim.x) {
+        const int r = i / TW, c = i - r * TW;
+        m[r * P + c] = sk[(r + 1) * kStW + 16 + c];
+    }
+    for (int i = threadIdx.x; i < TW + 2; i += blockDim.x) {
+        mN[i] = sk[15 + i];
+        mS[i] = sk[(TH + 1) * kStW + 15 + i];
+    }
+    for (int i = threadIdx.x; i < TH; i += blockDim.x) {
+        mW[i] = sk[(i + 1) * kStW + 15];
+        mE[i] = sk[(i + 1) * kStW + 16 + TW];
+    }
+    return ok;
+}
+
 // One pass over tile (tx, ty): load, alternate row / column phases over the
 // dirty lines until nothing changes, report which neighbours must run again,
 // write back.
@@ -800,7 +905,8 @@ __device__ void wl_seed_halo(TileWL<T, TW, TH, P> &sm, int dirty_in, bool conn8,
 // halo sides skips the phases and seeds the worklist from those sides.
 template <typename T, int TW, int TH, int P, int NW, bool HYB, bool WL, typename SM>
 __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, int cols, bool conn8, int tx, int ty,
-                                 int dirty_in, SM &sm, int seq_min, int wl_phases, long long budget, int *status) {
+                                 int dirty_in, SM &sm, int seq_min, int wl_phases, long long budget, int *status,
+                                 const TmaArgs &ta) {
     static_assert(!HYB || (std::is_same<T, uint8_t>::value && NW == TH / 32 && NW == TW / 32),
                   "lane-per-line scans: uint8, one warp per 32-line group");
     constexpr int NWORD = TW * TH / 32;
@@ -808,27 +914,36 @@ __device__ void cta_process_tile(const T *__restrict__ mask, T *out, int rows, i
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int y0 = ty * TH, x0 = tx * TW;
     T *o = sm.o;
-    // load tile + halo (image ring = 0) and the mask
-    for (int i = threadIdx.x; i < (TH + 2) * (TW + 2); i += NW * 32) {
-        int r = i / (TW + 2), cc = i - r * (TW + 2);
-        int y = y0 - 1 + r, x = x0 - 1 + cc;
-        o[r * P + cc] = (y >= 0 && y < rows && x >= 0 && x < cols) ? ldcg(out + (int64_t)y * cols + x) : (T)0;
+    bool tma_loaded = false;
+    if constexpr (std::is_same<T, uint8_t>::value && TW == 128 && TH == 128) {
+        if (ta.on) {
+            tma_tile_u8<P>(ta, tx, ty, o, sm.m, sm.mN, sm.mS, sm.mW, sm.mE, budget, status);
+            tma_loaded = true;
+        }
     }
-    for (int i = threadIdx.x; i < TH * TW; i += NW * 32) {
-        int r = i / TW, cc = i - r * TW;
-        int y = y0 + r, x = x0 + cc;
-        sm.m[r * P + cc] = (y < rows && x < cols) ? __ldg(mask + (int64_t)y * cols + x) : (T)0;
-    }
-    auto mask_at = [&](int y, int x) -> T {
-        return (y >= 0 && y < rows && x >= 0 && x < cols) ? __ldg(mask + (int64_t)y * cols + x) : (T)0;
-    };
-    for (int i = threadIdx.x; i < TW + 2; i += NW * 32) {
-        sm.mN[i] = mask_at(y0 - 1, x0 - 1 + i);
-        sm.mS[i] = mask_at(y0 + TH, x0 - 1 + i);
-    }
-    for (int i = threadIdx.x; i < TH; i += NW * 32) {
-        sm.mW[i] = mask_at(y0 + i, x0 - 1);
-        sm.mE[i] = mask_at(y0 + i, x0 + TW);
+    if (!tma_loaded) {
+        // load tile + halo (image ring = 0) and the mask
+        for (int i = threadIdx.x; i < (TH + 2) * (TW + 2); i += NW * 32) {
+            int r = i / (TW + 2), cc = i - r * (TW + 2);
+            int y = y0 - 1 + r, x = x0 - 1 + cc;
+            o[r * P + cc] = (y >= 0 && y < rows && x >= 0 && x < cols) ? ldcg(out + (int64_t)y * cols + x) : (T)0;
+        }
+        for (int i = threadIdx.x; i < TH * TW; i += NW * 32) {
+            int r = i / TW, cc = i - r * TW;
+            int y = y0 + r, x = x0 + cc;
+            sm.m[r * P + cc] = (y < rows && x < cols) ? __ldg(mask + (int64_t)y * cols + x) : (T)0;
+        }
+        auto mask_at = [&](int y, int x) -> T {
+            return (y >= 0 && y < rows && x >= 0 && x < cols) ? __ldg(mask + (int64_t)y * cols + x) : (T)0;
+        };
+        for (int i = threadIdx.x; i < TW + 2; i += NW * 32) {
+            sm.mN[i] = mask_at(y0 - 1, x0 - 1 + i);
+            sm.mS[i] = mask_at(y0 + TH, x0 - 1 + i);
+        }
+        for (int i = threadIdx.x; i < TH; i += NW * 32) {
+            sm.mW[i] = mask_at(y0 + i, x0 - 1);
+            sm.mE[i] = mask_at(y0 + i, x0 + TW);
+        }
     }
     const bool all = dirty_in & D_ALL;
     if (threadIdx.x < TH / 32) {
@@ -1408,13 +1523,45 @@ using TileOf = typename std::conditional<
 // MINB: CTAs per SM the register budget is sized for (8 warps: 4, i.e. at
 // most 64 registers a thread, so the reconstructions of several tiles in
 // flight can share an SM; 2 is kept as a tuning knob)
+// dynamic shared memory of a tile CTA: the tile struct, then (TMA form) the
+// two staging boxes, each on a 128-byte boundary (the base address is
+// rounded up at run time, hence the 128 bytes of slack), the mbarrier and
+// its phase
+template <typename Sm>
+constexpr size_t tile_smem_bytes(bool tma) {
+    return tma ? sizeof(Sm) + 128 + 2 * (size_t)kStagePitch + 16 : sizeof(Sm);
+}
+template <typename Sm>
+__device__ __forceinline__ uint8_t *tma_stage(unsigned char *sm_raw) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(sm_raw + sizeof(Sm));
+    return reinterpret_cast<uint8_t *>((a + 127) & ~(uintptr_t)127);
+}
+
 template <typename T, int TW, int TH, int P, int NW, bool PACKED, int MINB, bool HYB, bool WL>
 __global__ void __launch_bounds__(NW * 32, MINB) recon_cta(const T *__restrict__ mask, T *out, int rows, int cols,
-                                                           int conn, int tiles_x, int tiles_y, Queue q) {
-    extern __shared__ __align__(16) unsigned char sm_raw[];
+                                                           int conn, int tiles_x, int tiles_y, Queue q,
+                                                           const __grid_constant__ CUtensorMap out_map,
+                                                           const __grid_constant__ CUtensorMap mask_map, int use_tma) {
+    extern __shared__ __align__(128) unsigned char sm_raw[];
     using Sm = TileOf<T, TW, TH, P, NW, PACKED, WL>;
     Sm &sm = *reinterpret_cast<Sm *>(sm_raw);
     const bool conn8 = conn == 8;
+    TmaArgs ta{&out_map, &mask_map, nullptr, nullptr, nullptr, 0};
+    if (use_tma) {
+        ta.stage = tma_stage<Sm>(sm_raw);
+        ta.bar = reinterpret_cast<uint64_t *>(ta.stage + 2 * kStagePitch);
+        ta.phase = reinterpret_cast<unsigned *>(ta.bar + 1);
+        // self-check of the copy rules (destinations on 128-byte boundaries,
+        // barrier on 8): the plain loads run when they do not hold
+        ta.on = (reinterpret_cast<uintptr_t>(ta.stage) & 127) == 0 &&
+                ((reinterpret_cast<uintptr_t>(ta.stage) + kStagePitch) & 127) == 0 &&
+                (reinterpret_cast<uintptr_t>(ta.bar) & 7) == 0;
+        if (threadIdx.x == 0) {
+            mbar_init(ta.bar);
+            *ta.phase = 0;
+        }
+        __syncthreads();
+    }
     if constexpr (WL) {
         // the worklist starts empty (slot i free for ticket i) with nothing
         // queued; every tile pass leaves it empty
@@ -1439,7 +1586,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) recon_cta(const T *__restrict__
                 cta_process_tile_u8<TW, TH, NW>(mask, out, rows, cols, conn8, tx, ty, dirty, sm);
             else
                 cta_process_tile<T, TW, TH, P, NW, HYB, WL>(mask, out, rows, cols, conn8, tx, ty, dirty, sm, q.seq_min,
-                                                            q.wl_phases, q.budget, q.status);
+                                                            q.wl_phases, q.budget, q.status, ta);
             if constexpr (WL) {
                 // a worklist wait ran out of budget (DEV_TIMEOUT is set): leave;
                 // the other CTAs see the status word and leave too
@@ -1469,6 +1616,53 @@ __global__ void __launch_bounds__(NW * 32, MINB) recon_cta(const T *__restrict__
             __threadfence();
         }
     }
+}
+
+// TMA-fed tile loads on (default) or off (tuning knob NSG_RECON_TMA=0)
+bool recon_tma() {
+    if (const char *e = getenv("NSG_RECON_TMA")) return atoi(e) != 0;
+    return true;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no
+// link-time dependency on the driver library)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+// 2-D uint8 maps of `out` and `mask` (cols x rows, pitch cols) with the
+// 160 x 130 staging box; false when the layout does not allow it
+bool encode_u8_maps(void *out, const void *mask, int rows, int cols, CUtensorMap *om, CUtensorMap *mm) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn || cols % 16 != 0 || (reinterpret_cast<uintptr_t>(out) & 15) || (reinterpret_cast<uintptr_t>(mask) & 15))
+        return false;
+    const cuuint64_t dim[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t stride[1] = {(cuuint64_t)cols};
+    const cuuint32_t box[2] = {(cuuint32_t)kStW, (cuuint32_t)kStH};
+    const cuuint32_t estride[2] = {1, 1};
+    for (int k = 0; k < 2; ++k) {
+        CUtensorMap *m = k ? mm : om;
+        void *base = k ? const_cast<void *>(mask) : out;
+        if (fn(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, base, dim, stride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return false;
+    }
+    return true;
 }
 
 template <typename T, int TW, int TH, int P, int NW, bool PACKED = false, int MINB = (NW >= 16 && !PACKED) ? 1 : 2,
@@ -1540,7 +1734,17 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
         if (v >= 1 && v <= 8) q.wl_phases = v;
     }
     q.stats = c.ws.ctrl + C_RSTATS;
-    const size_t smem = sizeof(TileOf<T, TW, TH, P, NW, PACKED, WL>);
+    // TMA-fed tile loads (uint8, 128 x 128 lane-per-line form): tensor maps of
+    // the output plane and the mask, when their layout meets the tensor-map
+    // rules (16-byte aligned bases, row pitch a multiple of 16 bytes)
+    CUtensorMap out_map, mask_map;
+    memset(&out_map, 0, sizeof(out_map));
+    memset(&mask_map, 0, sizeof(mask_map));
+    int use_tma = 0;
+    if (std::is_same<T, uint8_t>::value && TW == 128 && TH == 128 && !PACKED && recon_tma())
+        use_tma = encode_u8_maps(out, mask, rows, cols, &out_map, &mask_map) ? 1 : 0;
+    using SmT = TileOf<T, TW, TH, P, NW, PACKED, WL>;
+    const size_t smem = tile_smem_bytes<SmT>(use_tma != 0);
     auto kfn = recon_cta<T, TW, TH, P, NW, PACKED, MINB, HYB, WL>;
     NSG_CUDA_TRY(c, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
@@ -1563,7 +1767,7 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
         if (v >= 1 && v < grid) grid = v;
     }
     if (grid > ntiles) grid = ntiles;
-    kfn<<<grid, NW * 32, smem, s>>>(mask, out, rows, cols, conn, tiles_x, tiles_y, q);
+    kfn<<<grid, NW * 32, smem, s>>>(mask, out, rows, cols, conn, tiles_x, tiles_y, q, out_map, mask_map, use_tma);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;

@@ -99,6 +99,7 @@ def test_imreconstruct_u8_rough(cuda, orc, shape, conn, wl, monkeypatch):
     {"NSG_RECON_HYB": "0"}, {"NSG_RECON_HYB": "0", "NSG_RECON_MINB": "2"}, {"NSG_RECON_WARPS": "16"},
     {"NSG_RECON_WARPS": "32"}, {"NSG_RECON_PACKED": "1", "NSG_RECON_HYB": "0"}, {"NSG_RECON_MAX_CTAS": "3"},
     {"NSG_RECON_WL": "1"}, {"NSG_RECON_WL": "1", "NSG_RECON_WLPH": "3"}, {"NSG_RECON_WL": "1", "NSG_RECON_MAX_CTAS": "2"},
+    {"NSG_RECON_TMA": "0"}, {"NSG_RECON_TMA": "0", "NSG_RECON_WL": "1"},
 ])
 @pytest.mark.parametrize("conn", [4, 8])
 def test_imreconstruct_u8_launch_forms(cuda, orc, conn, knobs, monkeypatch):
@@ -106,9 +107,12 @@ def test_imreconstruct_u8_launch_forms(cuda, orc, conn, knobs, monkeypatch):
     from nscale_gb300 import synth
     for k, v in knobs.items():
         monkeypatch.setenv(k, v)
-    marker, mask = synth.recon_inputs(700, 901, seed=0x5EED0021 + conn)
-    np.testing.assert_array_equal(N(MO.imreconstruct(T(marker), T(mask), conn)),
-                                  orc.imreconstruct(marker, mask, conn))
+    # 704 x 896: a width the tensor maps accept (TMA-fed tile loads), and
+    # 700 x 901: one they do not (plain loads)
+    for shape in ((704, 896), (700, 901)):
+        marker, mask = synth.recon_inputs(*shape, seed=0x5EED0021 + conn)
+        np.testing.assert_array_equal(N(MO.imreconstruct(T(marker), T(mask), conn)),
+                                      orc.imreconstruct(marker, mask, conn))
 
 
 @pytest.mark.parametrize("wl", ["0", "1"])
