@@ -54,6 +54,13 @@ ALG_BYTES_PER_PX = 137
 # dram__bytes_read.sum + dram__bytes_write.sum summed over every kernel of
 # one 2048 x 2048 tile run to SUCCESS (python -m nscale_gb300.tile_demo 2048)
 DRAM_BYTES_PER_PX = 413.6
+# the dominant kernel (largest share of the batched step): the uint8 grey
+# reconstruction, recon_cta<uint8>.  Algorithmic bytes: marker, mask read
+# once, output written once = 3 B/px.  Measured DRAM bytes per pixel of one
+# launch on the 2048 x 2048 pipeline input (ncu, profiles/), scaled to a
+# 4096 x 4096 launch by its pixels.
+RECON_ALG_BYTES_PER_PX = 3
+RECON_DRAM_BYTES_PER_PX = 2.08  # 8.55 MB read + 0.18 MB written, one launch, 2048 x 2048
 
 
 
@@ -378,6 +385,11 @@ def run_nsg(args, rank, world, local):
     pt_value = px / (pt_ms / 1e3) / 1e6
     ctx.close()
 
+    # ---- the dominant kernel alone: recon_cta<uint8> on the 4096^2
+    # pipeline input (rc_open, rc of one tile), CUDA events on the stream it
+    # is launched on
+    kernel = dominant_kernel(local)
+
     # ---- serving: Poisson arrivals of slide tiles into the server -----------
     serving = None
     if rank == 0 and args.serve_requests > 0:
@@ -436,13 +448,19 @@ def run_nsg(args, rank, world, local):
         "stage_ms_per_tile_pass": {k: round(v, 3) for k, v in per_stage.items() if v > 0},
         "stage_ms_per_tile_batched": {k: round(v / max(1, batched_timed), 3)
                                       for k, v in batched_stages.items() if v > 0},
-        "roofline": {"bound": "hbm", "kernel": "segmentNuclei pipeline, all stages (batched)",
-                     "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 5), "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_px": ALG_BYTES_PER_PX,
-                     "traffic": int(DRAM_BYTES_PER_PX * px),
-                     "traffic_note": f"DRAM bytes per step: {DRAM_BYTES_PER_PX} B/px measured by ncu over all "
-                                     f"kernels of one 2048x2048 tile, x pixels per step"},
+        "roofline": {"bound": "hbm", "kernel": kernel["kernel"], "achieved": kernel["achieved"], "peak": peak,
+                     "unit": "GB/s", "frac": round(kernel["achieved"] / peak, 6), "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": kernel["alg_bytes"], "ms_per_launch": kernel["ms"],
+                     "traffic": kernel["traffic"], "traffic_note": kernel["traffic_note"],
+                     "why": "propagation-latency bound (winding single-pixel paths through noise; the tile "
+                            "queue rescans lines), not bandwidth bound"},
+        "roofline_pipeline": {"bound": "hbm", "kernel": "segmentNuclei pipeline, all stages (batched)",
+                              "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                              "frac": round(achieved / peak, 5), "peak_kind": peak_kind,
+                              "algorithmic_bytes_per_px": ALG_BYTES_PER_PX,
+                              "traffic": int(DRAM_BYTES_PER_PX * px),
+                              "traffic_note": f"DRAM bytes per step: {DRAM_BYTES_PER_PX} B/px measured by ncu over "
+                                              f"all kernels of one 2048x2048 tile, x pixels per step"},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mpixel/s", "h2d_bytes_per_step": int(3 * px),
                 "d2h_bytes_per_step": int(4 * px), "tiles": len(tiles),
                 "form": "the same tiles from pinned host memory through nsg_segment_nuclei_batch (NSG_TILE_HOST)"},
@@ -456,6 +474,39 @@ def run_nsg(args, rank, world, local):
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
+
+
+def dominant_kernel(device):
+    """recon_cta<uint8> on the reconstruction input of one 4096 x 4096 tile
+    (marker = open(255 - R, disk19), mask = 255 - R): mean of 5 launches
+    timed with CUDA events on the stream the kernel runs on, after 3 warm-up
+    launches.  Achieved = algorithmic bytes (3 B/px) / launch time."""
+    import torch
+    from nscale_gb300 import morphologic_operations as MO
+    from nscale_gb300 import synth_torch
+    img = synth_torch.he_tile(4096, 4096, 0x5EED0000, device=f"cuda:{device}")
+    rc = (255 - img[..., 2]).contiguous()
+    rc_open = MO.morphOpen(rc, MO.disk19().numpy())
+    stream = torch.cuda.current_stream(device)  # the library launches on the caller's stream
+    for _ in range(3):
+        MO.imreconstruct(rc_open, rc, 8)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(5):
+        MO.imreconstruct(rc_open, rc, 8)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / 5
+    px = rc.numel()
+    alg = RECON_ALG_BYTES_PER_PX * px
+    traffic = int(RECON_DRAM_BYTES_PER_PX * px) if RECON_DRAM_BYTES_PER_PX else None
+    return {"kernel": "imreconstruct<uint8> call = recon_cta<uint8> + its min(marker, mask) init "
+                      "(4096x4096 pipeline input)",
+            "ms": round(ms, 3), "alg_bytes": alg, "achieved": round(alg / (ms / 1e3) / 1e9, 3),
+            "traffic": traffic,
+            "traffic_note": ("DRAM bytes per launch: ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                             "launch on the 2048x2048 input, scaled by pixels" if traffic else "not captured")}
 
 
 def pool_workers(args):
