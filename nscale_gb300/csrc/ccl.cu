@@ -91,21 +91,26 @@ __global__ void ccl_flatten(int *parent, int64_t n) {
         parent[i] = x;
     }
 }
-// the same, also clearing the per-component flag at every root (the first
-// step of the seed / border selections), and writing only changed links
-__global__ void ccl_flatten_zero(int *parent, int64_t n, int *__restrict__ flag) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int x0 = __ldcg(parent + i);
-        if (x0 < 0) continue;
-        int x = x0;
-        for (;;) {
-            int p = __ldcg(parent + x);
-            if (p == x) break;
-            x = p;
-        }
-        if (x != x0) parent[i] = x;
-        if (x == (int)i) flag[i] = 0;
+
+// The root of pixel i in a forest that was not flattened (-1 background).
+// After ccl_local every pixel points at its tile-local root and ccl_border
+// only hooks roots under smaller roots (or halves paths to ancestors), so
+// the chain is short and strictly decreasing.  With `write_back` the pixel's
+// link is replaced by its root when they differ: only final roots are
+// written, so another thread walking a chain through this pixel meets either
+// the old ancestor or the root, never a wrong node.  This is the flatten pass
+// folded into the first consumer of the labels.
+__device__ __forceinline__ int ccl_root(int *parent, int64_t i, bool write_back) {
+    const int x0 = __ldcg(parent + i);
+    if (x0 < 0) return x0;
+    int x = x0;
+    for (;;) {
+        const int p = __ldcg(parent + x);
+        if (p == x) break;
+        x = p;
     }
+    if (write_back && x != x0) parent[i] = x;
+    return x;
 }
 
 // ---- block-local union-find ------------------------------------------------
@@ -164,8 +169,12 @@ __device__ __forceinline__ void lunite(int *l, int a, int b) {
     }
 }
 
+// zero_at_roots (nullable): a per-pixel int plane whose entry at every local
+// root is set to 0 (the component flags or areas the consumers accumulate at
+// roots; every final root is a local root, so none is missed)
 template <typename Pred>
-__global__ void __launch_bounds__(256) ccl_local(Pred pr, int *__restrict__ parent, int rows, int cols, int conn) {
+__global__ void __launch_bounds__(256) ccl_local(Pred pr, int *__restrict__ parent, int rows, int cols, int conn,
+                                                 int *__restrict__ zero_at_roots) {
     __shared__ int l[LT * LT];
     const int x0 = blockIdx.x * LT, y0 = blockIdx.y * LT;
     const int tx = threadIdx.x & 31, tyb = threadIdx.x >> 5;  // 8 row groups
@@ -197,6 +206,7 @@ __global__ void __launch_bounds__(256) ccl_local(Pred pr, int *__restrict__ pare
         int r = l[li];
         if (r >= 0) {
             while (l[r] != r) r = l[r];
+            if (zero_at_roots && r == li) zero_at_roots[(int64_t)y * cols + x] = 0;
             r = (y0 + r / LT) * cols + (x0 + r % LT);
         }
         parent[(int64_t)y * cols + x] = r;
@@ -226,9 +236,10 @@ __global__ void ccl_border(Pred pr, int *parent, int rows, int cols, int conn, U
     }
 }
 
-__global__ void area_count(const int *__restrict__ lab, int *__restrict__ area, int64_t n) {
+// the first consumer of an unflattened forest: flattens it as it counts
+__global__ void area_count(int *lab, int *__restrict__ area, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        int l = lab[i];
+        int l = ccl_root(lab, i, true);
         // warp-aggregate pixels of the same component
         unsigned act = __activemask();
         unsigned same = __match_any_sync(act, l);
@@ -257,15 +268,17 @@ __global__ void area_select(const int *__restrict__ lab, const int *__restrict__
     }
 }
 
-// flag[root] |= seed present in the component
-__global__ void flag_seeds(const int *__restrict__ lab, const uint8_t *__restrict__ seed,
-                           const uint8_t *__restrict__ mask, int *__restrict__ flag, int64_t n) {
+// flag[root] |= seed present in the component; the first consumer of an
+// unflattened forest, so it flattens it on the way
+__global__ void flag_seeds(int *lab, const uint8_t *__restrict__ seed, const uint8_t *__restrict__ mask,
+                           int *__restrict__ flag, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        int l = lab[i];
+        int l = ccl_root(lab, i, true);
         if (l >= 0 && seed[i] && mask[i] && !__ldcg(flag + l)) flag[l] = 1;
     }
 }
-__global__ void flag_border(const int *__restrict__ lab, int *__restrict__ flag, int rows, int cols) {
+// reads an unflattened forest (roots found, nothing written back)
+__global__ void flag_border(int *lab, int *__restrict__ flag, int rows, int cols) {
     int64_t nb = 2 * (int64_t)cols + 2 * (int64_t)rows;
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nb; k += (int64_t)gridDim.x * blockDim.x) {
         int64_t i;
@@ -273,13 +286,9 @@ __global__ void flag_border(const int *__restrict__ lab, int *__restrict__ flag,
         else if (k < 2 * cols) i = (int64_t)(rows - 1) * cols + (k - cols);
         else if (k < 2 * cols + rows) i = (int64_t)(k - 2 * cols) * cols;
         else i = (int64_t)(k - 2 * cols - rows) * cols + (cols - 1);
-        int l = lab[i];
+        int l = ccl_root(lab, i, false);
         if (l >= 0) flag[l] = 1;
     }
-}
-__global__ void zero_flags_at_roots(const int *__restrict__ lab, int *__restrict__ flag, int64_t n) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        if (lab[i] == (int)i) flag[i] = 0;
 }
 // imreconstructBinary: marker pixels keep their value, reached mask pixels 255
 __global__ void select_recon(const int *__restrict__ lab, const int *__restrict__ flag,
@@ -300,11 +309,10 @@ __global__ void select_bw(const int *__restrict__ lab, const int *__restrict__ f
     }
 }
 // imfillHoles: pixels reached from the border through (img != 255) become 0,
-// everything else 255
-__global__ void select_fill(const int *__restrict__ lab, const int *__restrict__ flag, uint8_t *__restrict__ out,
-                            int64_t n) {
+// everything else 255 (reads an unflattened forest: the last consumer)
+__global__ void select_fill(int *lab, const int *__restrict__ flag, uint8_t *__restrict__ out, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        int l = lab[i];
+        int l = ccl_root(lab, i, false);
         out[i] = (l >= 0 && flag[l]) ? 0 : 255;
     }
 }
@@ -452,22 +460,23 @@ int exclusive_scan_i32(Ctx &c, const int32_t *in, int32_t *out, int64_t n, int32
     return NSG_SUCCESS;
 }
 
-// zero_flags (nullable): also clear flag[root] for every component root
+// zero_at_roots (nullable): a per-pixel int plane cleared at every component
+// root.  flatten = false leaves the forest unflattened: the caller's first
+// consumer finds roots itself (ccl_root) and writes them back.
 int ccl_u8(Ctx &c, const uint8_t *img, int32_t *parent, int rows, int cols, int conn, int mode, cudaStream_t s,
-           int *zero_flags) {
+           int *zero_at_roots, bool flatten) {
     int64_t n = (int64_t)rows * cols;
     PredU8 pr{img, mode};
     dim3 grid((cols + LT - 1) / LT, (rows + LT - 1) / LT);
-    ccl_local<PredU8><<<grid, 256, 0, s>>>(pr, parent, rows, cols, conn);
+    ccl_local<PredU8><<<grid, 256, 0, s>>>(pr, parent, rows, cols, conn, zero_at_roots);
     NSG_COUNT_LAUNCH();
     ccl_border<PredU8><<<blocks(c, n), kB, 0, s>>>(pr, parent, rows, cols, conn,
                                                    UfGuard{c.spin_budget, c.ws.ctrl + C_STATUS});
     NSG_COUNT_LAUNCH();
-    if (zero_flags)
-        ccl_flatten_zero<<<blocks(c, n), kB, 0, s>>>(parent, n, zero_flags);
-    else
+    if (flatten) {
         ccl_flatten<<<blocks(c, n), kB, 0, s>>>(parent, n);
-    NSG_COUNT_LAUNCH();
+        NSG_COUNT_LAUNCH();
+    }
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;
 }
@@ -477,7 +486,7 @@ int ccl_f32_masked(Ctx &c, const float *val, const uint8_t *valid, int32_t *pare
     int64_t n = (int64_t)rows * cols;
     PredF32 pr{val, valid};
     dim3 grid((cols + LT - 1) / LT, (rows + LT - 1) / LT);
-    ccl_local<PredF32><<<grid, 256, 0, s>>>(pr, parent, rows, cols, conn);
+    ccl_local<PredF32><<<grid, 256, 0, s>>>(pr, parent, rows, cols, conn, nullptr);
     NSG_COUNT_LAUNCH();
     ccl_border<PredF32><<<blocks(c, n), kB, 0, s>>>(pr, parent, rows, cols, conn,
                                                     UfGuard{c.spin_budget, c.ws.ctrl + C_STATUS});
@@ -493,8 +502,8 @@ int bwareaopen_dev(Ctx &c, const uint8_t *img, uint8_t *out, int rows, int cols,
                    int conn, int *d_count, cudaStream_t s) {
     int64_t n = (int64_t)rows * cols;
     int *lab = c.ws.i32[0], *area = c.ws.i32[1];
-    NSG_TRY(ccl_u8(c, img, lab, rows, cols, conn, CCL_EQUAL, s));
-    NSG_CUDA_TRY(c, cudaMemsetAsync(area, 0, n * sizeof(int), s));
+    // areas cleared at the roots by the labelling; area_count flattens the forest
+    NSG_TRY(ccl_u8(c, img, lab, rows, cols, conn, CCL_EQUAL, s, area, false));
     NSG_CUDA_TRY(c, cudaMemsetAsync(d_count, 0, sizeof(int), s));
     int g = blocks(c, n);
     area_count<<<g, kB, 0, s>>>(lab, area, n);
@@ -510,7 +519,7 @@ int recon_binary_dev(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t
                      cudaStream_t s) {
     int64_t n = (int64_t)rows * cols;
     int *lab = c.ws.i32[0], *flag = c.ws.i32[1];
-    NSG_TRY(ccl_u8(c, mask, lab, rows, cols, conn, CCL_NONZERO, s, flag));
+    NSG_TRY(ccl_u8(c, mask, lab, rows, cols, conn, CCL_NONZERO, s, flag, false));
     int g = blocks(c, n);
     flag_seeds<<<g, kB, 0, s>>>(lab, marker, mask, flag, n);
     NSG_COUNT_LAUNCH();
@@ -524,7 +533,7 @@ int bwselect_dev(Ctx &c, const uint8_t *bw, const uint8_t *seeds, uint8_t *out, 
                  cudaStream_t s) {
     int64_t n = (int64_t)rows * cols;
     int *lab = c.ws.i32[0], *flag = c.ws.i32[1];
-    NSG_TRY(ccl_u8(c, bw, lab, rows, cols, conn, CCL_NONZERO, s, flag));
+    NSG_TRY(ccl_u8(c, bw, lab, rows, cols, conn, CCL_NONZERO, s, flag, false));
     int g = blocks(c, n);
     flag_seeds<<<g, kB, 0, s>>>(lab, seeds, bw, flag, n);
     NSG_COUNT_LAUNCH();
@@ -537,7 +546,7 @@ int bwselect_dev(Ctx &c, const uint8_t *bw, const uint8_t *seeds, uint8_t *out, 
 int fill_holes_dev(Ctx &c, const uint8_t *img, uint8_t *out, int rows, int cols, int conn, cudaStream_t s) {
     int64_t n = (int64_t)rows * cols;
     int *lab = c.ws.i32[0], *flag = c.ws.i32[1];
-    NSG_TRY(ccl_u8(c, img, lab, rows, cols, conn, CCL_NOT255, s, flag));
+    NSG_TRY(ccl_u8(c, img, lab, rows, cols, conn, CCL_NOT255, s, flag, false));
     int g = blocks(c, n);
     flag_border<<<blocks(c, 2 * (int64_t)rows + 2 * cols), kB, 0, s>>>(lab, flag, rows, cols);
     NSG_COUNT_LAUNCH();
@@ -675,13 +684,9 @@ extern "C" int nsg_imfill_holes_u8_noalloc(const uint8_t *img, uint8_t *out, int
         cudaGetLastError();
         return NSG_ERR_CUDA;
     }
-    ccl_local<PredU8><<<grid, 256, 0, s>>>(pr, lab, rows, cols, conn);
+    ccl_local<PredU8><<<grid, 256, 0, s>>>(pr, lab, rows, cols, conn, flag);
     NSG_COUNT_LAUNCH();
     ccl_border<PredU8><<<g, kB, 0, s>>>(pr, lab, rows, cols, conn, UfGuard{noalloc_spin_budget(), sc.status});
-    NSG_COUNT_LAUNCH();
-    ccl_flatten<<<g, kB, 0, s>>>(lab, n);
-    NSG_COUNT_LAUNCH();
-    zero_flags_at_roots<<<g, kB, 0, s>>>(lab, flag, n);
     NSG_COUNT_LAUNCH();
     flag_border<<<noalloc_blocks(sc.sm_count, 2 * (int64_t)rows + 2 * cols), kB, 0, s>>>(lab, flag, rows, cols);
     NSG_COUNT_LAUNCH();

@@ -211,7 +211,7 @@ int recon_f32(Ctx &c, const float *marker, const float *mask, float *out, int ro
 // ccl.cu (uses i32[0..1] unless an output array doubles as the parent array)
 enum CclMode { CCL_EQUAL = 0, CCL_NONZERO = 1, CCL_NOT255 = 2 };
 int ccl_u8(Ctx &c, const uint8_t *img, int32_t *parent, int rows, int cols, int conn, int mode, cudaStream_t s,
-           int *zero_flags = nullptr);
+           int *zero_at_roots = nullptr, bool flatten = true);
 int ccl_f32_masked(Ctx &c, const float *val, const uint8_t *valid, int32_t *parent, int rows, int cols, int conn,
                    cudaStream_t s);
 int bwareaopen_dev(Ctx &c, const uint8_t *img, uint8_t *out, int rows, int cols, int min_size, int max_size,
