@@ -179,10 +179,16 @@ int morph_u8(Ctx &c, const uint8_t *in, uint8_t *out, int rows, int cols, const 
         size_t smem = (size_t)IH * IW + (size_t)nw * IH * TW;
         dim3 grid((cols + TW - 1) / TW, (rows + TH - 1) / TH);
         if (smem > 48 * 1024) {
+            // the device's opt-in maximum, the same from every caller: host
+            // threads that open with different elements never lower the limit
+            // under one another's launches
+            int optin = 0;
+            NSG_CUDA_TRY(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
+            if ((int64_t)smem > optin) return NSG_ERR_ARG;
             NSG_CUDA_TRY(c, cudaFuncSetAttribute(chord_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem));
+                                                 optin));
             NSG_CUDA_TRY(c, cudaFuncSetAttribute(chord_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem));
+                                                 optin));
         }
         if (is_max)
             chord_kernel<true><<<grid, kThreads, smem, s>>>(in, out, rows, cols, cs);

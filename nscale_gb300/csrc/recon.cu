@@ -1746,7 +1746,12 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
     using SmT = TileOf<T, TW, TH, P, NW, PACKED, WL>;
     const size_t smem = tile_smem_bytes<SmT>(use_tma != 0);
     auto kfn = recon_cta<T, TW, TH, P, NW, PACKED, MINB, HYB, WL>;
-    NSG_CUDA_TRY(c, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // The attribute is per kernel and process-wide, and the tiles of a batch
+    // run on several host threads, some with TMA staging and some without:
+    // every caller sets the same value (the larger, TMA size), so one
+    // thread's setting can never undercut another thread's launch.
+    NSG_CUDA_TRY(c, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)tile_smem_bytes<SmT>(true)));
     int per_sm = 0;
     NSG_CUDA_TRY(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, NW * 32, smem));
     // One CTA per SM by default (two for the 4-warp lane-per-line form): the
