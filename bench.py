@@ -52,15 +52,18 @@ METRIC = "segmentNuclei Mpixel/s on 1 GB300, batched vs per-tile; p50/p99 tile l
 ALG_BYTES_PER_PX = 137
 # measured DRAM reads + writes per pixel of the same pipeline: ncu
 # dram__bytes_read.sum + dram__bytes_write.sum summed over every kernel of
-# one 2048 x 2048 tile run to SUCCESS (python -m nscale_gb300.tile_demo 2048)
-DRAM_BYTES_PER_PX = 413.6
+# one 4096 x 4096 tile run to SUCCESS (python -m nscale_gb300.tile_demo 4096,
+# ncu --cache-control none: the caches as in a real run)
+DRAM_BYTES_PER_PX = 430.8
 # the dominant kernel (largest share of the batched step): the uint8 grey
-# reconstruction, recon_cta<uint8>.  Algorithmic bytes: marker, mask read
-# once, output written once = 3 B/px.  Measured DRAM bytes per pixel of one
-# launch on the 2048 x 2048 pipeline input (ncu, profiles/), scaled to a
-# 4096 x 4096 launch by its pixels.
+# reconstruction.  The timed call is nscale's imreconstruct: init_min_u8
+# (min(marker, mask) into the output) + recon_cta<uint8>.  Algorithmic bytes:
+# marker, mask read once, output written once = 3 B/px.  DRAM bytes of that
+# call on the 4096 x 4096 pipeline input, L2 flushed before each kernel (ncu
+# --cache-control all): init_min_u8 33.6 MB + recon_cta 34.8 MB; with warm
+# caches the two move 24.4 MB.
 RECON_ALG_BYTES_PER_PX = 3
-RECON_DRAM_BYTES_PER_PX = 2.08  # 8.55 MB read + 0.18 MB written, one launch, 2048 x 2048
+RECON_CALL_DRAM_BYTES = 68.4e6
 
 
 
@@ -460,7 +463,7 @@ def run_nsg(args, rank, world, local):
                               "algorithmic_bytes_per_px": ALG_BYTES_PER_PX,
                               "traffic": int(DRAM_BYTES_PER_PX * px),
                               "traffic_note": f"DRAM bytes per step: {DRAM_BYTES_PER_PX} B/px measured by ncu over "
-                                              f"all kernels of one 2048x2048 tile, x pixels per step"},
+                                              f"all kernels of one 4096x4096 tile (warm caches), x pixels per step"},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mpixel/s", "h2d_bytes_per_step": int(3 * px),
                 "d2h_bytes_per_step": int(4 * px), "tiles": len(tiles),
                 "form": "the same tiles from pinned host memory through nsg_segment_nuclei_batch (NSG_TILE_HOST)"},
@@ -500,13 +503,14 @@ def dominant_kernel(device):
     ms = ev0.elapsed_time(ev1) / 5
     px = rc.numel()
     alg = RECON_ALG_BYTES_PER_PX * px
-    traffic = int(RECON_DRAM_BYTES_PER_PX * px) if RECON_DRAM_BYTES_PER_PX else None
+    traffic = int(RECON_CALL_DRAM_BYTES) if px == 4096 * 4096 else None
     return {"kernel": "imreconstruct<uint8> call = recon_cta<uint8> + its min(marker, mask) init "
                       "(4096x4096 pipeline input)",
             "ms": round(ms, 3), "alg_bytes": alg, "achieved": round(alg / (ms / 1e3) / 1e9, 3),
             "traffic": traffic,
-            "traffic_note": ("DRAM bytes per launch: ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
-                             "launch on the 2048x2048 input, scaled by pixels" if traffic else "not captured")}
+            "traffic_note": ("DRAM bytes per call: ncu dram__bytes_read.sum + dram__bytes_write.sum of init_min_u8 + "
+                             "recon_cta<uint8> on this 4096x4096 input, L2 flushed before each kernel (24.4 MB with "
+                             "warm caches)" if traffic else "not captured")}
 
 
 def pool_workers(args):
