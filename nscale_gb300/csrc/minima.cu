@@ -20,8 +20,9 @@ namespace {
 
 constexpr int kB = 256;
 
-__global__ void hmin_prep(const float *__restrict__ img, float h, float *__restrict__ mask,
-                          float *__restrict__ marker, int64_t n) {
+// img may be the caller's output plane too (in-place imhmin): each thread
+// reads its pixel before writing it, so no __restrict__ on img / marker
+__global__ void hmin_prep(const float *img, float h, float *__restrict__ mask, float *marker, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         float m = -img[i];
         mask[i] = m;
@@ -32,6 +33,9 @@ __global__ void negate(float *__restrict__ a, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         a[i] = -a[i];
 }
+// c = the image (negated for minima); marker = c - 1, written straight into
+// the reconstruction's output (it is <= c everywhere, so it is already
+// min(marker, c)); ext_cand recomputes the same marker value from c
 __global__ void ext_prep(const float *__restrict__ img, bool neg, float *__restrict__ c, float *__restrict__ marker,
                          int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -40,10 +44,10 @@ __global__ void ext_prep(const float *__restrict__ img, bool neg, float *__restr
         marker[i] = __fadd_rn(v, -1.0f);
     }
 }
-__global__ void ext_cand(const float *__restrict__ marker, const float *__restrict__ rec, uint8_t *__restrict__ cand,
+__global__ void ext_cand(const float *__restrict__ c, const float *__restrict__ rec, uint8_t *__restrict__ cand,
                          int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        cand[i] = (marker[i] < rec[i]) ? 0 : 1;
+        cand[i] = (__fadd_rn(c[i], -1.0f) < rec[i]) ? 0 : 1;
 }
 __global__ void ext_zero_roots(const int *__restrict__ lab, int *__restrict__ flag, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -90,11 +94,14 @@ int blocks(Ctx &c, int64_t n) {
 // scratch: f32[0..1], recon's i32[5]
 int imhmin_dev(Ctx &c, const float *img, float *out, int rows, int cols, float h, int conn, cudaStream_t s) {
     int64_t n = (int64_t)rows * cols;
-    float *mask = c.ws.f32[0], *marker = c.ws.f32[1];
+    // h >= 0: the marker (mask - h <= mask) goes straight into the
+    // reconstruction's output, which is then already min(marker, mask)
+    const bool direct = h >= 0.0f;
+    float *mask = c.ws.f32[0], *marker = direct ? out : c.ws.f32[1];
     hmin_prep<<<blocks(c, n), kB, 0, s>>>(img, h, mask, marker, n);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
-    NSG_TRY(recon_f32(c, marker, mask, out, rows, cols, conn, s));
+    NSG_TRY(recon_f32(c, marker, mask, out, rows, cols, conn, s, direct));
     negate<<<blocks(c, n), kB, 0, s>>>(out, n);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
@@ -105,15 +112,15 @@ int imhmin_dev(Ctx &c, const float *img, float *out, int rows, int cols, float h
 int local_extrema_dev(Ctx &c, const float *img, uint8_t *out, int rows, int cols, int conn, bool minima,
                       cudaStream_t s) {
     int64_t n = (int64_t)rows * cols;
-    float *cim = c.ws.f32[0], *marker = c.ws.f32[1], *rec = c.ws.f32[2];
+    float *cim = c.ws.f32[0], *rec = c.ws.f32[2];
     uint8_t *cand = c.ws.u8[0];
     int *lab = c.ws.i32[0], *flag = c.ws.i32[1];
     int g = blocks(c, n);
-    ext_prep<<<g, kB, 0, s>>>(img, minima, cim, marker, n);
+    ext_prep<<<g, kB, 0, s>>>(img, minima, cim, rec, n);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
-    NSG_TRY(recon_f32(c, marker, cim, rec, rows, cols, conn, s));
-    ext_cand<<<g, kB, 0, s>>>(marker, rec, cand, n);
+    NSG_TRY(recon_f32(c, rec, cim, rec, rows, cols, conn, s, true));
+    ext_cand<<<g, kB, 0, s>>>(cim, rec, cand, n);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     NSG_TRY(ccl_f32_masked(c, cim, cand, lab, rows, cols, conn, s));

@@ -206,8 +206,10 @@ int morph_u8(Ctx &c, const uint8_t *in, uint8_t *out, int rows, int cols, const 
 // recon.cu (uses i32[5] for the tile queue)
 int recon_u8(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t *out, int rows, int cols, int conn,
              cudaStream_t s);
+// preinit: `out` already holds a marker that is <= mask at every pixel
+// (min(marker, mask) is then the marker itself and its pass is skipped)
 int recon_f32(Ctx &c, const float *marker, const float *mask, float *out, int rows, int cols, int conn,
-              cudaStream_t s);
+              cudaStream_t s, bool preinit = false);
 // ccl.cu (uses i32[0..1] unless an output array doubles as the parent array)
 enum CclMode { CCL_EQUAL = 0, CCL_NONZERO = 1, CCL_NOT255 = 2 };
 int ccl_u8(Ctx &c, const uint8_t *img, int32_t *parent, int rows, int cols, int conn, int mode, cudaStream_t s,

@@ -1667,7 +1667,8 @@ bool encode_u8_maps(void *out, const void *mask, int rows, int cols, CUtensorMap
 
 template <typename T, int TW, int TH, int P, int NW, bool PACKED = false, int MINB = (NW >= 16 && !PACKED) ? 1 : 2,
           bool HYB = false, bool WL = false>
-int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int cols, int conn, cudaStream_t s) {
+int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int cols, int conn, cudaStream_t s,
+                  bool preinit = false) {
     NSG_TRY(check_dims(c, rows, cols));
     NSG_TRY(check_conn(c, conn));
     const int64_t n = (int64_t)rows * cols;
@@ -1681,14 +1682,19 @@ int run_recon_cta(Ctx &c, const T *marker, const T *mask, T *out, int rows, int 
         c.last_error = "tile queue does not fit";
         return NSG_ERR_OOM;
     }
-    int blocks = (int)((n + 255) / 256);
-    if (blocks > c.sm_count * 16) blocks = c.sm_count * 16;
-    if (sizeof(T) == 1)
-        init_min_u8<<<blocks, 256, 0, s>>>((const uint8_t *)marker, (const uint8_t *)mask, (uint8_t *)out, n);
-    else
-        init_min_f32<<<blocks, 256, 0, s>>>((const float *)marker, (const float *)mask, (float *)out, n);
-    NSG_COUNT_LAUNCH();
-    NSG_LAUNCH_CHECK(c);
+    // out = min(marker, mask), unless the caller wrote a marker that is
+    // already <= mask everywhere into `out` (preinit): then min() is the
+    // marker itself, bit for bit, and the pass is skipped
+    if (!preinit) {
+        int blocks = (int)((n + 255) / 256);
+        if (blocks > c.sm_count * 16) blocks = c.sm_count * 16;
+        if (sizeof(T) == 1)
+            init_min_u8<<<blocks, 256, 0, s>>>((const uint8_t *)marker, (const uint8_t *)mask, (uint8_t *)out, n);
+        else
+            init_min_f32<<<blocks, 256, 0, s>>>((const float *)marker, (const float *)mask, (float *)out, n);
+        NSG_COUNT_LAUNCH();
+        NSG_LAUNCH_CHECK(c);
+    }
     // Whole-image row + column sweep pairs before the tile queue.  Off by
     // default: a thread per line walks the line serially, and on the tiles of
     // this pipeline a pair costs more than the tile passes it saves.
@@ -1834,17 +1840,18 @@ int recon_u8(Ctx &c, const uint8_t *marker, const uint8_t *mask, uint8_t *out, i
 }
 
 int recon_f32(Ctx &c, const float *marker, const float *mask, float *out, int rows, int cols, int conn,
-              cudaStream_t s) {
+              cudaStream_t s, bool preinit) {
     const int nw = recon_warps();
     if (nw == 8) {
         if (recon_worklist(c) && !getenv("NSG_RECON_WARPS"))
             return run_recon_cta<float, 64, 64, 67, 8, false, 4, false, true>(c, marker, mask, out, rows, cols, conn,
-                                                                              s);
-        if (recon_minb() == 2) return run_recon_cta<float, 64, 64, 67, 8, false, 2>(c, marker, mask, out, rows, cols, conn, s);
-        return run_recon_cta<float, 64, 64, 67, 8, false, 4>(c, marker, mask, out, rows, cols, conn, s);
+                                                                              s, preinit);
+        if (recon_minb() == 2)
+            return run_recon_cta<float, 64, 64, 67, 8, false, 2>(c, marker, mask, out, rows, cols, conn, s, preinit);
+        return run_recon_cta<float, 64, 64, 67, 8, false, 4>(c, marker, mask, out, rows, cols, conn, s, preinit);
     }
-    if (nw == 32) return run_recon_cta<float, 64, 64, 67, 32>(c, marker, mask, out, rows, cols, conn, s);
-    return run_recon_cta<float, 64, 64, 67, 16>(c, marker, mask, out, rows, cols, conn, s);
+    if (nw == 32) return run_recon_cta<float, 64, 64, 67, 32>(c, marker, mask, out, rows, cols, conn, s, preinit);
+    return run_recon_cta<float, 64, 64, 67, 16>(c, marker, mask, out, rows, cols, conn, s, preinit);
 }
 
 }  // namespace nsg

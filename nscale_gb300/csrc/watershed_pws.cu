@@ -182,7 +182,7 @@ __global__ void k_classify(PW a) {
         a.uown[p] = -1;
         a.rlocal[p] = -1;
         a.rparent[p] = -2;
-        a.isroot[p] = 0;
+        // (isroot is written for every pixel by k_roots, after the labelling)
     }
 }
 
