@@ -222,3 +222,27 @@ def test_server_budget_split_over_classes(cuda):
         assert cw[b] == 1
     finally:
         srv.close()
+
+
+def test_pool_mixed_staging_widths_stress(cuda):
+    """Tiles whose width is a multiple of 16 take the TMA-staged
+    reconstruction (larger dynamic shared memory); the others take plain
+    loads.  Many workers launching both forms at once must never fail a
+    launch or change a label (the kernel's shared-memory limit is process-wide
+    and set by every caller)."""
+    import torch
+    from nscale_gb300 import synth_torch
+    from nscale_gb300.serving import TilePool
+    shapes = [(384, 512), (384, 500), (256, 768), (256, 771)] * 6
+    tiles = [synth_torch.he_tile(r, c, 0x5EED7200 + i, device="cuda") for i, (r, c) in enumerate(shapes)]
+    want = [_single(t.cpu().numpy()) for t in tiles]
+    pool = TilePool(384, 771, workers=12)
+    try:
+        for _ in range(3):
+            got = pool.segment(tiles)
+            for (ws, wl, wn, _wb), (gs, gl, gn, _gb) in zip(want, got):
+                assert gs == ws and gn == wn
+                assert np.array_equal(gl.cpu().numpy(), wl)
+    finally:
+        pool.close()
+    torch.cuda.synchronize()
