@@ -12,6 +12,8 @@
 //        plateaus (union-find), flag a plateau when any of its pixels has a
 //        strictly greater conn-neighbour (out-of-image = -FLT_MAX, never
 //        greater), keep the unflagged candidates.
+#include <float.h>
+
 #include "nsg_internal.cuh"
 
 namespace nsg {
@@ -28,6 +30,23 @@ __global__ void hmin_prep(const float *img, float h, float *__restrict__ mask, f
         mask[i] = m;
         marker[i] = __fadd_rn(m, -h);
     }
+}
+// the segmentation's imhmin input built from the distance transform: the
+// pipeline's distance is -dist inside seg_big and -FLT_MAX outside
+// (HistologicalEntities.cpp:366-374) and imhmin negates it again, so the
+// reconstruction's mask is dist / FLT_MAX directly (negation is exact)
+__global__ void hmin_prep_dist(const float *__restrict__ dist, const uint8_t *__restrict__ seg, float h,
+                               float *__restrict__ mask, float *__restrict__ marker, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float m = seg[i] ? dist[i] : FLT_MAX;
+        mask[i] = m;
+        marker[i] = __fadd_rn(m, -h);
+    }
+}
+// maxima: the candidates' marker c - 1, the image itself serving as c
+__global__ void ext_marker(const float *__restrict__ c, float *__restrict__ marker, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        marker[i] = __fadd_rn(c[i], -1.0f);
 }
 __global__ void negate(float *__restrict__ a, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -108,15 +127,39 @@ int imhmin_dev(Ctx &c, const float *img, float *out, int rows, int cols, float h
     return NSG_SUCCESS;
 }
 
-// scratch: f32[0..2], u8[0], i32[0..1], recon's i32[5]
+// The pipeline's imhmin, kept negated: out = -imhmin(distance, h, conn) where
+// distance = -dist inside seg and -FLT_MAX outside.  imhmin negates its
+// input, reconstructs and negates back, and watershed2's localMinima negates
+// the result once more; here the negations fold away (each is exact), the
+// reconstruction's output is returned as it is, and the watershed takes its
+// minima as the maxima of this plane.  scratch: f32[0], recon's i32[5]
+int imhmin_neg_dist_dev(Ctx &c, const float *dist, const uint8_t *seg, float *out, int rows, int cols, float h,
+                        int conn, cudaStream_t s) {
+    if (!(h >= 0.0f)) return NSG_ERR_ARG;  // the marker must stay <= the mask
+    int64_t n = (int64_t)rows * cols;
+    float *mask = c.ws.f32[0];
+    hmin_prep_dist<<<blocks(c, n), kB, 0, s>>>(dist, seg, h, mask, out, n);
+    NSG_COUNT_LAUNCH();
+    NSG_LAUNCH_CHECK(c);
+    return recon_f32(c, out, mask, out, rows, cols, conn, s, true);
+}
+
+// scratch: f32[0] (minima) and f32[2], u8[0], i32[0..1], recon's i32[5]
 int local_extrema_dev(Ctx &c, const float *img, uint8_t *out, int rows, int cols, int conn, bool minima,
                       cudaStream_t s) {
     int64_t n = (int64_t)rows * cols;
-    float *cim = c.ws.f32[0], *rec = c.ws.f32[2];
+    float *rec = c.ws.f32[2];
     uint8_t *cand = c.ws.u8[0];
     int *lab = c.ws.i32[0], *flag = c.ws.i32[1];
     int g = blocks(c, n);
-    ext_prep<<<g, kB, 0, s>>>(img, minima, cim, rec, n);
+    // c = the image for maxima (read in place), its negation for minima
+    const float *cim = img;
+    if (minima) {
+        ext_prep<<<g, kB, 0, s>>>(img, true, c.ws.f32[0], rec, n);
+        cim = c.ws.f32[0];
+    } else {
+        ext_marker<<<g, kB, 0, s>>>(img, rec, n);
+    }
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     NSG_TRY(recon_f32(c, rec, cim, rec, rows, cols, conn, s, true));

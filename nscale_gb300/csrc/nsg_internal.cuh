@@ -196,7 +196,6 @@ int diff_threshold(Ctx &c, const uint8_t *rc, const uint8_t *rc_recon, int rows,
 int and_not(Ctx &c, uint8_t *inout, const uint8_t *notmask, int64_t n, cudaStream_t s);
 int mask_copy_bgr(Ctx &c, const uint8_t *bgr, int64_t row_stride, const uint8_t *mask, int rows, int cols,
                   uint8_t *out, cudaStream_t s);
-int neg_dist_mask(Ctx &c, const float *dist, const uint8_t *mask, int64_t n, float *out, cudaStream_t s);
 int invert_u8_dev(Ctx &c, const uint8_t *in, uint8_t *out, int64_t n, cudaStream_t s);
 template <typename T>
 int invert_dev(Ctx &c, const T *in, T *out, int64_t n, cudaStream_t s);  // uint8_t, int32_t, float
@@ -232,11 +231,15 @@ int exclusive_scan_i32(Ctx &c, const int32_t *in, int32_t *out, int64_t n, int32
 int dist_transform_dev(Ctx &c, const uint8_t *mask, float *dist, int rows, int cols, cudaStream_t s);
 // minima.cu (uses f32[0..2], i32[0..1], u8[0])
 int imhmin_dev(Ctx &c, const float *img, float *out, int rows, int cols, float h, int conn, cudaStream_t s);
+int imhmin_neg_dist_dev(Ctx &c, const float *dist, const uint8_t *seg, float *out, int rows, int cols, float h,
+                        int conn, cudaStream_t s);
 int local_extrema_dev(Ctx &c, const float *img, uint8_t *out, int rows, int cols, int conn, bool minima,
                       cudaStream_t s);
 // watershed.cu (uses i32[2..4], u8[0..2])
+// img_negated: `img` holds the negation of watershed2's image (its minima
+// are then the maxima of `img`)
 int watershed_dev(Ctx &c, const uint8_t *bgr, const float *img, int32_t *out, int rows, int cols, int conn,
-                  cudaStream_t s);
+                  cudaStream_t s, bool img_negated = false);
 // watershed_pws.cu: domain-parallel exact Meyer flooding of a padded marker
 // image (markers > 0, unknown 0, negative reset to 0) with packed BGR colours.
 // Writes the flooded labels into outp (padded); falls back to the serial

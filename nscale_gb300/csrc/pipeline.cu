@@ -213,15 +213,18 @@ int segment_nuclei_dev(Ctx &c, const uint8_t *bgr, int64_t stride, int rows, int
     NSG_TRY(morph_u8(c, P[5], P[6], rows, cols, kCross3, 3, true, s));  // seg_big
     t_mark(c, 10, s);
     NSG_TRY(dist_transform_dev(c, P[6], c.ws.p_f32[0], rows, cols, s));
-    NSG_TRY(neg_dist_mask(c, c.ws.p_f32[0], P[6], n, c.ws.p_f32[1], s));
     t_mark(c, 11, s);
-    NSG_TRY(imhmin_dev(c, c.ws.p_f32[1], c.ws.p_f32[0], rows, cols, 1.0f, 8, s));  // HE:384 (hard-coded 8)
+    // distance = -dist inside seg_big, -FLT_MAX outside (HE:366-374); imhmin(distance, 1, 8) (HE:384, hard-coded
+    // 8).  imhmin negates, reconstructs and negates back, and watershed2's localMinima negates again: the
+    // negations are folded (each is exact), p_f32[1] holds -imhmin(distance), and the watershed below takes its
+    // minima as the maxima of that plane.
+    NSG_TRY(imhmin_neg_dist_dev(c, c.ws.p_f32[0], P[6], c.ws.p_f32[1], rows, cols, 1.0f, 8, s));
     t_mark(c, 12, s);
     NSG_TRY(take_counts(c));
     if (c.ws.h_ctrl[C_COUNT1] == 0) return fail_fill(NSG_NO_CANDIDATES_LEFT);
     uint8_t *nuclei = (uint8_t *)c.ws.p_i32[0];
     NSG_TRY(mask_copy_bgr(c, bgr, stride, P[6], rows, cols, nuclei, s));
-    NSG_TRY(watershed_dev(c, nuclei, c.ws.p_f32[0], c.ws.p_i32[1], rows, cols, p.watershedConnectivity, s));
+    NSG_TRY(watershed_dev(c, nuclei, c.ws.p_f32[1], c.ws.p_i32[1], rows, cols, p.watershedConnectivity, s, true));
     keep_ge0<<<g, kB, 0, s>>>(P[6], c.ws.p_i32[1], P[7], n);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);

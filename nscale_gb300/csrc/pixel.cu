@@ -168,12 +168,6 @@ __global__ void mask_copy_bgr_kernel(const uint8_t *__restrict__ bgr, int64_t st
     }
 }
 
-__global__ void neg_dist_mask_kernel(const float *__restrict__ d, const uint8_t *__restrict__ m, int64_t n,
-                                     float *__restrict__ out) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        out[i] = m[i] ? -d[i] : -FLT_MAX;
-}
-
 // PixelOperations::invert<T> (PixelOperations.cpp:22-43): unsigned
 // max - x, signed ~x + 1 (two's-complement negation, wrapping), float -x as
 // the reference's scaled copy x * -1 + 0 (so +0 stays +0)
@@ -279,13 +273,6 @@ int mask_copy_bgr(Ctx &c, const uint8_t *bgr, int64_t stride, const uint8_t *m, 
                   cudaStream_t s) {
     int64_t n = (int64_t)rows * cols;
     mask_copy_bgr_kernel<<<blocks_for(c, n), kBlock, 0, s>>>(bgr, stride, m, rows, cols, out);
-    NSG_COUNT_LAUNCH();
-    NSG_LAUNCH_CHECK(c);
-    return NSG_SUCCESS;
-}
-
-int neg_dist_mask(Ctx &c, const float *d, const uint8_t *m, int64_t n, float *out, cudaStream_t s) {
-    neg_dist_mask_kernel<<<blocks_for(c, n), kBlock, 0, s>>>(d, m, n, out);
     NSG_COUNT_LAUNCH();
     NSG_LAUNCH_CHECK(c);
     return NSG_SUCCESS;

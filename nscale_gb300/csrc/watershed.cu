@@ -63,11 +63,12 @@ int blocks(Ctx &c, int64_t n) {
 // i32[2] minima labels; i32[3] padded markers; i32[4] padded colours;
 // i32[0] padded flood result; the watershed workspace.
 int watershed_dev(Ctx &c, const uint8_t *bgr, const float *img, int32_t *out, int rows, int cols, int conn,
-                  cudaStream_t s) {
+                  cudaStream_t s, bool img_negated) {
     uint8_t *minima = c.ws.u8[1];
     int *labels = c.ws.i32[2], *mk = c.ws.i32[3], *outp = c.ws.i32[0];
     uint32_t *colp = (uint32_t *)c.ws.i32[4];
-    NSG_TRY(local_extrema_dev(c, img, minima, rows, cols, conn, true, s));
+    // localMinima(img) is localMaxima(-img) (MorphologicOperations.cpp:3839)
+    NSG_TRY(local_extrema_dev(c, img, minima, rows, cols, conn, !img_negated, s));
     NSG_TRY(bwlabel_dev(c, minima, labels, rows, cols, conn, s));
     int64_t np = (int64_t)(rows + 2) * (cols + 2);
     ws_pack<<<blocks(c, np), 256, 0, s>>>(labels, bgr, rows, cols, mk, colp);
