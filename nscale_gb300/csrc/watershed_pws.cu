@@ -275,20 +275,25 @@ __device__ __forceinline__ void q_push(Q &q, int *next, int lvl, int e) {
     q.t[lvl] = e;
 }
 
-// P1: flood domain d to completion, U pixels are dummies.  One warp per
-// block; each thread keeps its queue heads and tails in shared memory (a
-// row of kQPitch ints, odd, so that threads at the same level hit different
-// banks): every pop and push touches them, and thread-private local memory
-// would share the L1 with the flood's global reads.
-constexpr int kP1Threads = 32, kQPitch = 513;
+// P1: flood domain d to completion, U pixels are dummies.  A flood is a
+// serial program whose every pop takes its own path (dummy or pixel, how
+// many neighbours it pushes, which level comes next), so floods sharing a
+// warp diverge on every pop and run one after another: each block runs ONE
+// flood on one thread, and the SM's warp scheduler interleaves the floods
+// instead (measured on 64 tiles, one at a time: P1 468 / 383 / 304 / 271 ms
+// and P3 316 / 238 / 144 / 109 ms with 32 / 8 / 2 / 1 floods per block).
+// The flood keeps its queue heads and tails in shared memory (kQPitch ints):
+// every pop and push touches them, and thread-private local memory would
+// share the L1 with the flood's global reads.
+constexpr int kP1Threads = 1, kQPitch = 513;
 constexpr size_t kP1Smem = sizeof(int) * kP1Threads * kQPitch;
 __device__ void phase1_domain(const PW &a, int d, Q &q);
-// Size-ordered dispatch.  A flood block holds its shared memory (32 queue
-// tables) until its longest flood ends, so blocks are filled with floods of
-// about the same length, longest first: the ids are bucketed by work class
-// (the leading-zero count of the work: a factor of two per class) and thread
-// t of the launch takes the t-th id.  Which thread floods which domain does
-// not change any result (every flood writes only its own domain's records).
+// Size-ordered dispatch: the floods start longest first, so that the longest
+// chains are not left to the end of the launch: the ids are bucketed by work
+// class (the leading-zero count of the work: a factor of two per class) and
+// thread t of the launch takes the t-th id.  Which thread floods which domain
+// does not change any result (every flood writes only its own domain's
+// records).
 // mode 0: domains, work = pixels + reserved dummy slots (P1);
 // mode 1: P3 groups (mcount > 0), work = their members' pixels.
 __device__ __forceinline__ int flood_work(const PW &a, int d, int mode) {
@@ -1633,10 +1638,9 @@ static int launch_bfs(Ctx &c, const PW &a, const uint8_t *nbm, cudaStream_t s) {
 // The dispatch list of the P1 (mode 0) or P3 (mode 1) floods, longest
 // first, and its length on the host (*count; a readback, so this waits for
 // the stream).  The flood kernels are launched with exactly the blocks that
-// have floods: each block holds 32 queue tables of shared memory, and a
-// launch padded with empty blocks would wait, under load from the other
-// tiles in flight, until every empty block found that much free shared
-// memory on some SM.
+// have floods: each block holds a queue table of shared memory, and a launch
+// padded with empty blocks would wait, under load from the other tiles in
+// flight, until every empty block found room on some SM.
 static int order_floods(Ctx &c, PW &a, int mode, int *count, cudaStream_t s) {
     const int g = blocks(c, a.n);
     NSG_CUDA_TRY(c, cudaMemsetAsync(a.obucket, 0, 64 * sizeof(int), s));
