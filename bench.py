@@ -54,7 +54,7 @@ ALG_BYTES_PER_PX = 137
 # dram__bytes_read.sum + dram__bytes_write.sum summed over every kernel of
 # one 4096 x 4096 tile run to SUCCESS (python -m nscale_gb300.tile_demo 4096,
 # ncu --cache-control none: the caches as in a real run)
-DRAM_BYTES_PER_PX = 430.8
+DRAM_BYTES_PER_PX = 384.7
 # the dominant kernel (largest share of the batched step): the uint8 grey
 # reconstruction.  The timed call is nscale's imreconstruct: init_min_u8
 # (min(marker, mask) into the output) + recon_cta<uint8>.  Algorithmic bytes:
