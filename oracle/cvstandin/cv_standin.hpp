@@ -1,7 +1,7 @@
 // cv_standin.hpp — a minimal, header-only stand-in for the few OpenCV 2.4
 // types and calls that nscale's own morphology / pixel functions use, so that
 // those functions can be compiled from the nscale sources and run as a
-// checker of the oracle (test infrastructure only; OpenCV is not installed).
+// reference build that checks the oracle (test infrastructure only; OpenCV is not installed).
 //
 // Only what the compiled nscale functions touch is here: a reference-counted
 // row-major Mat with ROI views, Mat_<T>, Size / Range / Rect / Scalar,

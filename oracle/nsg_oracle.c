@@ -1,7 +1,7 @@
 /*
  * nsg_oracle.c — CPU restatement of nscale's segmentNuclei hot path.
  *
- * TEST INFRASTRUCTURE ONLY (the checker).  Never linked into the product.
+ * TEST INFRASTRUCTURE ONLY (the oracle).  Never linked into the product.
  * Single-threaded, plain C11, written to follow the reference's sequential
  * algorithms step by step so that it can serve as the parity oracle.
  *

@@ -1,7 +1,7 @@
 /*
  * nsg_oracle.h — CPU restatement of nscale's segmentNuclei path.
  *
- * TEST INFRASTRUCTURE ONLY. This library is the checker that the CUDA path is
+ * TEST INFRASTRUCTURE ONLY. This library is the oracle that the CUDA path is
  * compared against; it is never linked into, called by, or shipped with the
  * product library (libnsg.so).  Only tests/, __graft_entry__.smoke() and the
  * cpu_baseline / --impl reference legs of bench.py may load it.

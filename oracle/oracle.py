@@ -1,11 +1,11 @@
 """ctypes wrapper over the CPU oracle (oracle/_build/libnsg_oracle.so) and the
-two checkers built from nscale's own code: ConnComponents
+two reference libraries built from nscale's own code: ConnComponents
 (oracle/_ref/libnsg_refcc.so) and the nscale morphology / pixel functions of
 the segmentNuclei path compiled against an OpenCV stand-in
 (oracle/_ref/libnsg_refnscale.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
-CPU legs of bench.py as the checker.  The product path never imports it.
+CPU legs of bench.py, to check results.  The product path never imports it.
 """
 from __future__ import annotations
 
@@ -67,7 +67,7 @@ def nscale_src() -> str:
 
 def build(ref: bool | None = None) -> None:
     """Compile the oracle (and, when the nscale sources are present, the two
-    checkers made from nscale's own code into oracle/_ref)."""
+    reference libraries made from nscale's own code into oracle/_ref)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
     src = nscale_src()
     if ref is None:

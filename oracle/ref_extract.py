@@ -1,4 +1,4 @@
-"""Build step of the reference checker (test infrastructure only): writes the
+"""Build step of the reference library (test infrastructure only): writes the
 definitions of nscale's own CPU functions on the segmentNuclei path, taken
 verbatim from the nscale sources at build time, into one include file under
 oracle/_ref/ (git-ignored).  oracle/ref_nscale_wrap.cpp compiles them against

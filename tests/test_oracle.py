@@ -1,4 +1,4 @@
-"""CPU tests of the oracle (the checker): pinned against the reference's own
+"""CPU tests of the oracle: pinned against the reference's own
 ConnComponents outputs (tests/golden/cc_golden.npz, generated by
 tests/golden/make_golden.py from src/segment/ConnComponents.cpp), against
 independent scipy implementations, and on known-answer cases."""
