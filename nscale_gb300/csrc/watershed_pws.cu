@@ -820,7 +820,9 @@ __global__ void __launch_bounds__(kBfsThreads) k_bfs(PW a, const uint8_t *__rest
             }
             __syncthreads();
         }
-        int seg = 0;
+        // the segment of the chunk's first entry: this CTA's own in a local
+        // layer (no walk over the counts), else found by the walk below
+        int seg = local ? me : 0;
         const int pt = (cnt + kBfsThreads - 1) / kBfsThreads;
         const int j0 = threadIdx.x * pt;
         unsigned long long win = 0;
