@@ -214,24 +214,39 @@ __global__ void __launch_bounds__(256) ccl_local(Pred pr, int *__restrict__ pare
 }
 
 // unions of neighbour pairs that cross a tile border (backward neighbours:
-// left, up, up-left, up-right, the pairs ConnComponents::label visits)
+// left, up, up-left, up-right, the pairs ConnComponents::label visits).
+// One block per 32x32 tile, one thread per pixel that can have such a pair:
+// the tile's top row (32), its left and right columns below it (31 + 31).
+// Union-find hooks the larger root under the smaller, so the final roots do
+// not depend on the order of the unions.
+constexpr int kBorderPx = LT + 2 * (LT - 1);  // 94
 template <typename Pred>
-__global__ void ccl_border(Pred pr, int *parent, int rows, int cols, int conn, UfGuard ug) {
-    int64_t n = (int64_t)rows * cols;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        int y = (int)(i / cols), x = (int)(i - (int64_t)y * cols);
-        int bx = x & (LT - 1), by = y & (LT - 1);
-        if (bx != 0 && by != 0 && bx != LT - 1) continue;
-        if (!pr.fg(i)) continue;
-        if (x > 0 && bx == 0 && pr.joins(i, i - 1)) unite(parent, (int)i, (int)(i - 1), ug);
-        if (y > 0) {
-            int64_t u = i - cols;
-            if (by == 0 && pr.joins(i, u)) unite(parent, (int)i, (int)u, ug);
-            if (conn == 8) {
-                if (x > 0 && (bx == 0 || by == 0) && pr.joins(i, u - 1)) unite(parent, (int)i, (int)(u - 1), ug);
-                if (x < cols - 1 && (bx == LT - 1 || by == 0) && pr.joins(i, u + 1))
-                    unite(parent, (int)i, (int)(u + 1), ug);
-            }
+__global__ void __launch_bounds__(128) ccl_border(Pred pr, int *parent, int rows, int cols, int conn, UfGuard ug) {
+    const int t = threadIdx.x;
+    if (t >= kBorderPx) return;
+    int bx, by;
+    if (t < LT) {
+        bx = t;
+        by = 0;
+    } else if (t < 2 * LT - 1) {
+        bx = 0;
+        by = t - (LT - 1);
+    } else {
+        bx = LT - 1;
+        by = t - (2 * LT - 2);
+    }
+    const int x = blockIdx.x * LT + bx, y = blockIdx.y * LT + by;
+    if (x >= cols || y >= rows) return;
+    const int64_t i = (int64_t)y * cols + x;
+    if (!pr.fg(i)) return;
+    if (x > 0 && bx == 0 && pr.joins(i, i - 1)) unite(parent, (int)i, (int)(i - 1), ug);
+    if (y > 0) {
+        const int64_t u = i - cols;
+        if (by == 0 && pr.joins(i, u)) unite(parent, (int)i, (int)u, ug);
+        if (conn == 8) {
+            if (x > 0 && (bx == 0 || by == 0) && pr.joins(i, u - 1)) unite(parent, (int)i, (int)(u - 1), ug);
+            if (x < cols - 1 && (bx == LT - 1 || by == 0) && pr.joins(i, u + 1))
+                unite(parent, (int)i, (int)(u + 1), ug);
         }
     }
 }
@@ -470,8 +485,7 @@ int ccl_u8(Ctx &c, const uint8_t *img, int32_t *parent, int rows, int cols, int 
     dim3 grid((cols + LT - 1) / LT, (rows + LT - 1) / LT);
     ccl_local<PredU8><<<grid, 256, 0, s>>>(pr, parent, rows, cols, conn, zero_at_roots);
     NSG_COUNT_LAUNCH();
-    ccl_border<PredU8><<<blocks(c, n), kB, 0, s>>>(pr, parent, rows, cols, conn,
-                                                   UfGuard{c.spin_budget, c.ws.ctrl + C_STATUS});
+    ccl_border<PredU8><<<grid, 128, 0, s>>>(pr, parent, rows, cols, conn, UfGuard{c.spin_budget, c.ws.ctrl + C_STATUS});
     NSG_COUNT_LAUNCH();
     if (flatten) {
         ccl_flatten<<<blocks(c, n), kB, 0, s>>>(parent, n);
@@ -488,8 +502,7 @@ int ccl_f32_masked(Ctx &c, const float *val, const uint8_t *valid, int32_t *pare
     dim3 grid((cols + LT - 1) / LT, (rows + LT - 1) / LT);
     ccl_local<PredF32><<<grid, 256, 0, s>>>(pr, parent, rows, cols, conn, nullptr);
     NSG_COUNT_LAUNCH();
-    ccl_border<PredF32><<<blocks(c, n), kB, 0, s>>>(pr, parent, rows, cols, conn,
-                                                    UfGuard{c.spin_budget, c.ws.ctrl + C_STATUS});
+    ccl_border<PredF32><<<grid, 128, 0, s>>>(pr, parent, rows, cols, conn, UfGuard{c.spin_budget, c.ws.ctrl + C_STATUS});
     NSG_COUNT_LAUNCH();
     ccl_flatten<<<blocks(c, n), kB, 0, s>>>(parent, n);
     NSG_COUNT_LAUNCH();
@@ -686,7 +699,7 @@ extern "C" int nsg_imfill_holes_u8_noalloc(const uint8_t *img, uint8_t *out, int
     }
     ccl_local<PredU8><<<grid, 256, 0, s>>>(pr, lab, rows, cols, conn, flag);
     NSG_COUNT_LAUNCH();
-    ccl_border<PredU8><<<g, kB, 0, s>>>(pr, lab, rows, cols, conn, UfGuard{noalloc_spin_budget(), sc.status});
+    ccl_border<PredU8><<<grid, 128, 0, s>>>(pr, lab, rows, cols, conn, UfGuard{noalloc_spin_budget(), sc.status});
     NSG_COUNT_LAUNCH();
     flag_border<<<noalloc_blocks(sc.sm_count, 2 * (int64_t)rows + 2 * cols), kB, 0, s>>>(lab, flag, rows, cols);
     NSG_COUNT_LAUNCH();
