@@ -12,7 +12,7 @@ lane-per-line scan: raster then anti-raster step, neighbours read as they are)
 and tiles in a random order, with small tiles so that propagation crosses many
 of them, and compares with the oracle's reconstruction.
 
-The worklist form (the default) is modelled too: a whole-tile pass runs one
+The worklist form (a tuning option, off by default) is modelled too: a whole-tile pass runs one
 row + column phase pair and then a pixel worklist seeded with the pixels the
 column phase changed; a pass for changed halo sides skips the phases and
 seeds the worklist from the edge pixels those sides can raise.  Pixels are
